@@ -1,0 +1,1385 @@
+// gpx_explore.cu -- GB300 (sm_103a) on-the-fly state-space exploration.
+//
+// One persistent cooperative kernel explores a network of LTSs level by level
+// (breadth-first), replacing the reference's host relaunch loop
+// (GPUexplore.cu:2109-2142) and its gather / gather_por kernels
+// (GPUexplore.cu:756-1189, 1191-1733):
+//
+//  * Frontier: all visited states live in an append-only state store in HBM
+//    (the BFS queue); level L is the index range [lo, hi).  Warps claim chunks
+//    of the range with one atomic, stage a batch of states in shared memory and
+//    expand them.  The reference instead sweeps the whole hash table for
+//    NEW-flagged entries (GPUexplore.cu:812-855).
+//  * Successor generation: a batch's (state, process) pairs are spread over the
+//    warp's lanes.  A lane decodes its process's local state, emits the local
+//    successors, and resolves the synchronisation rules it leads (it is the
+//    lowest participant) by looking up the other participants' transition
+//    groups, then enumerates the rule's Cartesian product (GPUexplore.cu:904-1122).
+//    Successors go through a per-warp queue in shared memory and are probed 32
+//    at a time, one per lane, fully converged.
+//  * Visited set: a bucketised multi-choice hash table of 32/64/128-bit slots;
+//    a bucket is one 32-byte DRAM sector (64 bytes for 128-bit slots), read with
+//    one 256-bit load; insertion claims the first empty slot in probe order with
+//    one atomicCAS of the whole key, so a state is stored exactly once without
+//    locks (the reference writes a multi-word vector word by word,
+//    GPUexplore.cu:393-440).
+//  * Levels end at a grid barrier whose last arriver closes the level (records
+//    its count, checks violations, the state budget and errors).  Every wait is
+//    bounded and reports GPX_ERR_TIMEOUT instead of hanging.
+//  * Cluster POR (GPUexplore.cu:1345-1675): per state, per-process clusters,
+//    proviso bits, closure and the smallest valid cluster are computed by the
+//    warp; with the cycle proviso a first grid-wide pass looks every successor
+//    up in the table (which holds exactly the states of earlier levels) before a
+//    second pass inserts the kept successors.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cinttypes>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "gpx.h"
+#include "gpx_model.h"
+
+struct gpx_model {
+    gpx::Gpf gpf;
+    gpx::Decoded dec;
+};
+
+namespace gpx {
+
+// ------------------------------------------------------------------ constants
+
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+constexpr int kQcap = 64;       // per-warp successor queue (entries)
+constexpr int kPairMax = 256;   // (state, process) pairs staged per warp batch
+constexpr int kMaxProbe = 32;   // buckets probed before reporting the table full
+constexpr uint32_t kMaxLevels = 1u << 20;
+
+enum Mode : int { MODE_PLAIN = 0, MODE_POR = 1, MODE_PROVISO = 2 };
+enum Phase : uint32_t { PH_EXPAND = 0, PH_DECIDE = 1 };
+
+// Control block shared by all blocks of the persistent kernel.
+struct Ctrl {
+    unsigned long long store_count; // states appended to the store
+    unsigned long long lo, hi;      // the level being expanded: store indices [lo, hi)
+    unsigned long long cursor;      // next unclaimed offset within [lo, hi)
+    unsigned long long lookups, probes, expanded, inserts, inserts_lookups;
+    unsigned int claim;             // states per claim
+    unsigned int level;             // BFS depth of [lo, hi)
+    unsigned int nlevels;           // recorded level counts
+    unsigned int done;              // exploration finished
+    unsigned int pause;             // launch budget (-k) reached: kernel returns, host relaunches
+    unsigned int violation;         // property violated during this level
+    unsigned int error;             // gpx_status
+    unsigned int stop;              // gpx_stop
+    unsigned int phase;             // Phase
+    unsigned int launch_levels;     // levels closed in this launch
+    unsigned int bar_count, bar_gen;
+    unsigned int timeout_at;        // where a bounded wait gave up (diagnostics)
+};
+
+struct Params {
+    void *table;
+    unsigned long long nbuckets;
+    void *store;
+    unsigned long long store_cap;
+    const uint32_t *model; // device layout (gpx_model.h)
+    uint32_t model_words;
+    uint32_t model_in_smem;
+    uint32_t *sel;         // per-frontier-state cluster (cycle proviso)
+    unsigned long long *levels;
+    Ctrl *ctrl;
+    unsigned long long seed;
+    unsigned long long max_states;
+    unsigned long long timeout_ns;
+    uint32_t property;
+    uint32_t levels_per_launch;
+    uint32_t total_warps;
+};
+
+// ------------------------------------------------------------- device helpers
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) { // SplitMix64 finaliser (Steele, Lea, Flood 2014)
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ uint64_t globaltimer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void ld256_cg(const void *p, uint32_t (&w)[8]) {
+    asm volatile("ld.global.cg.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
+                 : "l"(p));
+}
+
+__device__ __forceinline__ uint64_t lmask(uint32_t w) { return (w >= 64) ? ~0ull : ((1ull << w) - 1ull); }
+
+// Keys are stored in slot form: the packed state vector plus an occupancy
+// marker in the top bit of each 32/64-bit half, so an all-zero slot is empty
+// and the all-zero state vector is a valid key.
+struct K32 { uint32_t v; };
+struct K64 { unsigned long long v; };
+struct __align__(16) K128 { unsigned long long lo, hi; };
+
+template <class K> struct KT;
+
+template <> struct KT<K32> {
+    static constexpr int kSlots = 8; // 32-byte bucket
+    __device__ static K32 initial() { return {0x80000000u}; }
+    __device__ static bool eq(const K32 &a, const K32 &b) { return a.v == b.v; }
+    __device__ static bool empty(const K32 &a) { return a.v == 0; }
+    __device__ static bool torn(const K32 &) { return false; }
+    __device__ static uint32_t get(const K32 &k, uint32_t f, uint32_t w) { return (k.v >> f) & (uint32_t)lmask(w); }
+    __device__ static void set(K32 &k, uint32_t f, uint32_t w, uint32_t x) {
+        uint32_t m = (uint32_t)lmask(w) << f;
+        k.v = (k.v & ~m) | ((x << f) & m);
+    }
+    __device__ static uint64_t hash(const K32 &k, uint64_t seed) { return mix64((uint64_t)k.v ^ seed); }
+    __device__ static K32 cas(K32 *p, K32 cmp, K32 val) { return {atomicCAS(&p->v, cmp.v, val.v)}; }
+    __device__ static void bucket(const K32 *b, K32 (&s)[kSlots]) {
+        uint32_t w[8];
+        ld256_cg(b, w);
+#pragma unroll
+        for (int j = 0; j < 8; j++) s[j].v = w[j];
+    }
+    __device__ static K32 load(const K32 *p) { return {__ldcg(&p->v)}; }
+    __device__ static void words(const K32 &k, uint32_t (&w)[4]) {
+        w[0] = k.v & 0x7FFFFFFFu;
+        w[1] = w[2] = w[3] = 0;
+    }
+};
+
+template <> struct KT<K64> {
+    static constexpr int kSlots = 4; // 32-byte bucket
+    __device__ static K64 initial() { return {0x8000000000000000ull}; }
+    __device__ static bool eq(const K64 &a, const K64 &b) { return a.v == b.v; }
+    __device__ static bool empty(const K64 &a) { return a.v == 0; }
+    __device__ static bool torn(const K64 &) { return false; }
+    __device__ static uint32_t get(const K64 &k, uint32_t f, uint32_t w) { return (uint32_t)((k.v >> f) & lmask(w)); }
+    __device__ static void set(K64 &k, uint32_t f, uint32_t w, uint32_t x) {
+        unsigned long long m = lmask(w) << f;
+        k.v = (k.v & ~m) | (((unsigned long long)x << f) & m);
+    }
+    __device__ static uint64_t hash(const K64 &k, uint64_t seed) { return mix64(k.v ^ seed); }
+    __device__ static K64 cas(K64 *p, K64 cmp, K64 val) { return {atomicCAS(&p->v, cmp.v, val.v)}; }
+    __device__ static void bucket(const K64 *b, K64 (&s)[kSlots]) {
+        uint32_t w[8];
+        ld256_cg(b, w);
+#pragma unroll
+        for (int j = 0; j < 4; j++) s[j].v = (unsigned long long)w[2 * j] | ((unsigned long long)w[2 * j + 1] << 32);
+    }
+    __device__ static K64 load(const K64 *p) { return {__ldcg(&p->v)}; }
+    __device__ static void words(const K64 &k, uint32_t (&w)[4]) {
+        unsigned long long v = k.v & 0x7FFFFFFFFFFFFFFFull;
+        w[0] = (uint32_t)v;
+        w[1] = (uint32_t)(v >> 32);
+        w[2] = w[3] = 0;
+    }
+};
+
+// 128-bit slots hold 63 state bits in each 64-bit half (bit 63 of both halves
+// is the occupancy marker).  Each half is read atomically, so a slot caught in
+// the middle of its insertion shows exactly one zero half ("torn"); such a slot
+// is re-read with an atomic before it is judged.
+template <> struct KT<K128> {
+    static constexpr int kSlots = 4; // 64-byte bucket
+    static constexpr unsigned long long kOcc = 0x8000000000000000ull;
+    __device__ static K128 initial() { return {kOcc, kOcc}; }
+    __device__ static bool eq(const K128 &a, const K128 &b) { return a.lo == b.lo && a.hi == b.hi; }
+    __device__ static bool empty(const K128 &a) { return (a.lo | a.hi) == 0; }
+    __device__ static bool torn(const K128 &a) { return (a.lo == 0) != (a.hi == 0); }
+    __device__ static uint32_t get(const K128 &k, uint32_t f, uint32_t w) {
+        if (f + w <= 63) return (uint32_t)((k.lo >> f) & lmask(w));
+        if (f >= 63) return (uint32_t)((k.hi >> (f - 63)) & lmask(w));
+        uint32_t nlo = 63 - f;
+        return (uint32_t)(((k.lo >> f) & lmask(nlo)) | ((k.hi & lmask(w - nlo)) << nlo));
+    }
+    __device__ static void set(K128 &k, uint32_t f, uint32_t w, uint32_t x) {
+        if (f + w <= 63) {
+            unsigned long long m = lmask(w) << f;
+            k.lo = (k.lo & ~m) | (((unsigned long long)x << f) & m);
+        } else if (f >= 63) {
+            unsigned long long m = lmask(w) << (f - 63);
+            k.hi = (k.hi & ~m) | (((unsigned long long)x << (f - 63)) & m);
+        } else {
+            uint32_t nlo = 63 - f;
+            unsigned long long ml = lmask(nlo) << f, mh = lmask(w - nlo);
+            k.lo = (k.lo & ~ml) | (((unsigned long long)x << f) & ml);
+            k.hi = (k.hi & ~mh) | (((unsigned long long)x >> nlo) & mh);
+        }
+    }
+    __device__ static uint64_t hash(const K128 &k, uint64_t seed) { return mix64(k.lo ^ mix64(k.hi ^ seed)); }
+    __device__ static K128 cas(K128 *p, K128 cmp, K128 val) {
+        unsigned long long olo, ohi;
+        asm volatile(
+            "{\n\t.reg .b128 c, v, o;\n\t"
+            "mov.b128 c, {%2, %3};\n\t"
+            "mov.b128 v, {%4, %5};\n\t"
+            "atom.global.cas.b128 o, [%6], c, v;\n\t"
+            "mov.b128 {%0, %1}, o;\n\t}"
+            : "=l"(olo), "=l"(ohi)
+            : "l"(cmp.lo), "l"(cmp.hi), "l"(val.lo), "l"(val.hi), "l"(p)
+            : "memory");
+        return {olo, ohi};
+    }
+    __device__ static void bucket(const K128 *b, K128 (&s)[kSlots]) {
+        uint32_t w[8];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            ld256_cg(b + 2 * h, w);
+            s[2 * h].lo = (unsigned long long)w[0] | ((unsigned long long)w[1] << 32);
+            s[2 * h].hi = (unsigned long long)w[2] | ((unsigned long long)w[3] << 32);
+            s[2 * h + 1].lo = (unsigned long long)w[4] | ((unsigned long long)w[5] << 32);
+            s[2 * h + 1].hi = (unsigned long long)w[6] | ((unsigned long long)w[7] << 32);
+        }
+    }
+    __device__ static K128 load(const K128 *p) {
+        return {__ldcg(&p->lo), __ldcg(&p->hi)};
+    }
+    __device__ static void words(const K128 &k, uint32_t (&w)[4]) {
+        unsigned long long lo = k.lo & ~kOcc, hi = k.hi & ~kOcc;
+        w[0] = (uint32_t)lo;
+        w[1] = (uint32_t)(lo >> 32) | (uint32_t)((hi & 1ull) << 31);
+        w[2] = (uint32_t)(hi >> 1);
+        w[3] = (uint32_t)(hi >> 33);
+    }
+};
+
+__device__ __forceinline__ unsigned long long bucket_of(uint64_t h, int i, unsigned long long nb) {
+    uint64_t x = i ? mix64(h + (uint64_t)i * 0x9E3779B97F4A7C15ull) : h;
+    return __umul64hi(x, nb);
+}
+
+// Find-or-insert.  Returns 0 if the key was present, 1 if this call inserted
+// it, 2 if every probed bucket was full.  Slots go from empty to a key exactly
+// once; every caller scans the same probe sequence and claims the first empty
+// slot it sees with a full-key CAS, so two insertions of one key always meet in
+// the same slot and exactly one wins.
+template <class K>
+__device__ __forceinline__ int find_or_insert(K *table, unsigned long long nb, const K &key, uint64_t h,
+                                              unsigned int &probes) {
+    constexpr int S = KT<K>::kSlots;
+    for (int i = 0; i < kMaxProbe; i++) {
+        K *b = table + bucket_of(h, i, nb) * S;
+        K s[S];
+        KT<K>::bucket(b, s);
+        probes++;
+#pragma unroll
+        for (int j = 0; j < S; j++)
+            if (KT<K>::eq(s[j], key)) return 0;
+#pragma unroll
+        for (int j = 0; j < S; j++) {
+            if (KT<K>::empty(s[j]) || KT<K>::torn(s[j])) {
+                K zero;
+                memset(&zero, 0, sizeof zero);
+                K old = KT<K>::cas(b + j, zero, key);
+                if (KT<K>::empty(old)) return 1;
+                if (KT<K>::eq(old, key)) return 0;
+            }
+        }
+    }
+    return 2;
+}
+
+// Lookup in a table no one writes to during the call (the decide pass of the
+// cycle proviso): an empty slot on the probe path means the key is absent.
+template <class K>
+__device__ __forceinline__ bool find_key(K *table, unsigned long long nb, const K &key, uint64_t h,
+                                         unsigned int &probes) {
+    constexpr int S = KT<K>::kSlots;
+    for (int i = 0; i < kMaxProbe; i++) {
+        K *b = table + bucket_of(h, i, nb) * S;
+        K s[S];
+        KT<K>::bucket(b, s);
+        probes++;
+#pragma unroll
+        for (int j = 0; j < S; j++) {
+            K v = s[j];
+            if (KT<K>::torn(v)) {
+                K zero;
+                memset(&zero, 0, sizeof zero);
+                v = KT<K>::cas(b + j, zero, zero); // atomic re-read; writes nothing new
+            }
+            if (KT<K>::eq(v, key)) return true;
+            if (KT<K>::empty(v)) return false;
+        }
+    }
+    return false;
+}
+
+// --------------------------------------------------------- per-warp scratch
+
+template <class K> struct WarpScratch {
+    K keys[32];                 // the batch's source states
+    uint32_t appl[kPairMax];    // per pair: applicable rules among those it leads (bit r)
+    uint32_t cl0[kPairMax];     // per pair: static POR cluster
+    uint32_t clo[kPairMax];     // per pair: cluster closure
+    uint32_t en[32], prov[32], sel[32], best[32];
+    K qkey[kQcap];              // successor queue
+    uint32_t qg[kQcap], qmask[kQcap];
+};
+
+struct WarpStats {
+    unsigned int lookups, probes, inserts, expanded, ilookups;
+    unsigned int violation;
+};
+
+// Model accessors over the device layout (gpx_model.h).
+struct MView {
+    const uint32_t *w;
+    uint32_t n;
+    __device__ uint32_t fb(uint32_t p) const { return w[H_FB + p]; }
+    __device__ uint32_t bs(uint32_t p) const { return w[H_BS + p]; }
+    __device__ const uint32_t *rec(uint32_t p, uint32_t s) const {
+        return w + w[H_OFF_RECS] + (w[H_PSBASE + p] + s) * kRecWords;
+    }
+    __device__ uint32_t ltgt(uint32_t i) const { return w[w[H_OFF_LTGT] + i]; }
+    __device__ uint32_t stgt(uint32_t i) const { return w[w[H_OFF_STGT] + i]; }
+    __device__ uint32_t lrule(uint32_t i) const { return w[w[H_OFF_LRULE] + i]; }
+    __device__ uint32_t rmask(uint32_t k) const { return w[w[H_OFF_RULES] + 2 * k]; }
+    __device__ uint32_t ract(uint32_t k) const { return w[w[H_OFF_RULES] + 2 * k + 1]; }
+    // synchronising group of (p, s) for action a: {action, toff, tcnt, has1} or null
+    __device__ const uint32_t *group(const uint32_t *rec, uint32_t a) const {
+        const uint32_t *g = w + w[H_OFF_SENT] + rec[R_SOFF] * 4;
+        for (uint32_t i = 0; i < rec[R_SCNT]; i++, g += 4) {
+            if (g[0] == a) return g;
+            if (g[0] > a) break;
+        }
+        return nullptr;
+    }
+};
+
+__device__ __forceinline__ void set_error(Ctrl *c, unsigned int code) { atomicCAS(&c->error, 0u, code); }
+
+__device__ __forceinline__ unsigned int vload(const unsigned int *p) { return *(volatile const unsigned int *)p; }
+__device__ __forceinline__ unsigned long long vload(const unsigned long long *p) {
+    return *(volatile const unsigned long long *)p;
+}
+
+// Close the phase that every block has just finished (run by the last block to
+// arrive at the barrier, with all other blocks waiting).
+template <int MODE> __device__ void close_phase(const Params &P) {
+    Ctrl *c = P.ctrl;
+    if (MODE == MODE_PROVISO && c->phase == PH_DECIDE) {
+        c->phase = PH_EXPAND;
+        c->cursor = 0;
+        return;
+    }
+    unsigned long long hi = c->hi;
+    unsigned long long newhi = c->store_count;
+    if (newhi > P.store_cap) newhi = P.store_cap;
+    unsigned long long cnt = newhi - hi;
+    if (cnt) {
+        if (c->nlevels < kMaxLevels)
+            P.levels[c->nlevels++] = cnt;
+        else
+            set_error(c, GPX_ERR_UNSUPPORTED);
+    }
+    c->level++;
+    c->launch_levels++;
+    if (c->error) {
+        c->done = 1;
+        c->stop = GPX_STOP_ERROR;
+    } else if (c->violation) {
+        c->done = 1;
+        c->stop = GPX_STOP_VIOLATION;
+    } else if (cnt == 0) {
+        c->done = 1;
+        c->stop = GPX_STOP_DONE;
+    } else if (P.max_states && newhi >= P.max_states) {
+        c->done = 1;
+        c->stop = GPX_STOP_BUDGET;
+    }
+    c->lo = hi;
+    c->hi = newhi;
+    c->cursor = 0;
+    c->phase = (MODE == MODE_PROVISO) ? PH_DECIDE : PH_EXPAND;
+    unsigned long long per = cnt / ((unsigned long long)P.total_warps * 4ull);
+    c->claim = (unsigned int)(per < 32 ? 32 : (per > 4096 ? 4096 : per));
+    if (P.levels_per_launch && c->launch_levels >= P.levels_per_launch && !c->done) c->pause = 1;
+}
+
+// Grid-wide barrier; the last block to arrive closes the phase.  The wait is
+// bounded: after timeout_ns it records GPX_ERR_TIMEOUT and returns.
+template <int MODE> __device__ void grid_barrier(const Params &P) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Ctrl *c = P.ctrl;
+        unsigned int gen = vload(&c->bar_gen);
+        __threadfence();
+        unsigned int arrived = atomicAdd(&c->bar_count, 1u);
+        if (arrived == gridDim.x - 1) {
+            __threadfence();
+            close_phase<MODE>(P);
+            c->bar_count = 0;
+            __threadfence();
+            atomicAdd(&c->bar_gen, 1u);
+        } else {
+            uint64_t t0 = globaltimer();
+            unsigned int ns = 32;
+            while (vload(&c->bar_gen) == gen) {
+                __nanosleep(ns);
+                if (ns < 1024) ns <<= 1;
+                if (globaltimer() - t0 > P.timeout_ns) {
+                    set_error(c, GPX_ERR_TIMEOUT);
+                    atomicMax(&c->timeout_at, 1u);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------- the kernel
+
+template <class K, int MODE> struct Explorer {
+    const Params &P;
+    MView M;
+    WarpScratch<K> &ws;
+    K *table;
+    K *store;
+    uint32_t lane;
+    uint32_t lanemask_lt;
+    WarpStats st;
+    bool safety, deadlock;
+
+    __device__ Explorer(const Params &p, const uint32_t *model, WarpScratch<K> &w)
+        : P(p), ws(w), table((K *)p.table), store((K *)p.store) {
+        M.w = model;
+        M.n = model[H_NPROCS];
+        lane = threadIdx.x & 31;
+        lanemask_lt = (1u << lane) - 1u;
+        st = WarpStats{0, 0, 0, 0, 0, 0};
+        safety = P.property == GPX_PROP_SAFETY;
+        deadlock = P.property == GPX_PROP_DEADLOCK;
+    }
+
+    // Drain `cnt` (<= 32) queue entries starting at `head`: one lookup per lane.
+    __device__ void drain(uint32_t head, uint32_t cnt, bool lookup_mode) {
+        bool valid = lane < cnt;
+        uint32_t pos = (head + lane) % kQcap;
+        int res = -1;
+        K key;
+        if (valid) {
+            key = ws.qkey[pos];
+            uint64_t h = KT<K>::hash(key, P.seed);
+            if (lookup_mode) {
+                bool found = find_key<K>(table, P.nbuckets, key, h, st.probes);
+                // cycle proviso: a successor satisfies it unless it is an explored
+                // ("OLD") state -- every state in the table during this pass
+                if (!found) atomicOr(&ws.prov[ws.qg[pos]], ws.qmask[pos]);
+            } else {
+                res = find_or_insert<K>(table, P.nbuckets, key, h, st.probes);
+                if (res == 2) set_error(P.ctrl, GPX_ERR_TABLE_FULL);
+            }
+        }
+        st.lookups += cnt;
+        if (lookup_mode) return;
+        st.ilookups += cnt;
+        uint32_t ins = __ballot_sync(kFull, res == 1);
+        if (ins) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(&P.ctrl->store_count, (unsigned long long)__popc(ins));
+            base = __shfl_sync(kFull, base, 0);
+            if (res == 1) {
+                unsigned long long idx = base + __popc(ins & lanemask_lt);
+                if (idx < P.store_cap)
+                    store[idx] = key;
+                else
+                    set_error(P.ctrl, GPX_ERR_STORE_FULL);
+            }
+            st.inserts += __popc(ins);
+        }
+    }
+
+    // Expand a batch of B states store[first .. first+B).
+    __device__ void batch(unsigned long long first, uint32_t B, unsigned long long lvl_off, bool decide) {
+        const uint32_t n = M.n;
+        if (lane < B) {
+            ws.keys[lane] = KT<K>::load(store + first + lane);
+            ws.en[lane] = 0;
+            ws.prov[lane] = 0;
+            ws.best[lane] = kFull;
+            ws.sel[lane] = kFull;
+        }
+        __syncwarp();
+        const uint32_t npairs = B * n;
+        const bool check = (MODE != MODE_PROVISO) || decide;
+
+        // A: enabledness, applicable rules, static clusters, safety on moves into monitor state 1
+        for (uint32_t i = lane; i < npairs; i += 32) {
+            uint32_t g = i / n, p = i - g * n;
+            K key = ws.keys[g];
+            uint32_t s = KT<K>::get(key, M.fb(p), M.bs(p));
+            const uint32_t *rec = M.rec(p, s);
+            uint32_t lcnt = rec[R_LCNT], roff = rec[R_ROFF], rcnt = rec[R_RCNT];
+            uint32_t appl = 0, provbits = lcnt ? (1u << p) : 0u;
+            bool viol = safety && check && p == n - 1 && (rec[R_FLAGS] & 1u);
+            for (uint32_t r = 0; r < rcnt; r++) {
+                uint32_t k = M.lrule(roff + r);
+                uint32_t mask = M.rmask(k), act = M.ract(k);
+                bool ok = true, hit1 = false;
+                uint32_t rest = mask;
+                while (rest) {
+                    uint32_t q = __ffs(rest) - 1;
+                    rest &= rest - 1;
+                    uint32_t sq = (q == p) ? s : KT<K>::get(key, M.fb(q), M.bs(q));
+                    const uint32_t *grp = M.group(q == p ? rec : M.rec(q, sq), act);
+                    if (!grp) {
+                        ok = false;
+                        break;
+                    }
+                    if (q == n - 1 && grp[3]) hit1 = true;
+                }
+                if (ok) {
+                    appl |= 1u << r;
+                    provbits |= mask;
+                    if (safety && check && hit1) viol = true;
+                }
+            }
+            ws.appl[i] = appl;
+            if (MODE != MODE_PLAIN) ws.cl0[i] = rec[R_CL0];
+            if (lcnt | appl) ws.en[g] = 1;
+            if (MODE == MODE_POR) atomicOr(&ws.prov[g], provbits);
+            if (viol) st.violation = 1;
+        }
+        __syncwarp();
+        if (deadlock && check && lane < B && ws.en[lane] == 0) st.violation = 1;
+        if (check && lane < B) st.expanded++;
+
+        // B: cluster selection (POR without cycle proviso, from enabledness)
+        if (MODE == MODE_POR) select_clusters(B);
+        if (MODE == MODE_PROVISO && !decide) {
+            if (lane < B) ws.sel[lane] = __ldcg(P.sel + lvl_off + lane);
+            __syncwarp();
+        }
+
+        // C: emit successors (all of them when deciding, else those of the selected cluster)
+        emit(B, decide);
+
+        if (MODE == MODE_PROVISO && decide) {
+            select_clusters(B);
+            if (lane < B) P.sel[lvl_off + lane] = ws.sel[lane];
+        }
+        __syncwarp();
+    }
+
+    // Smallest valid cluster per state (GPUexplore.cu:1633-1672); ws.prov holds
+    // the proviso bits, ws.cl0 the static clusters.
+    __device__ void select_clusters(uint32_t B) {
+        const uint32_t n = M.n;
+        __syncwarp();
+        const uint32_t npairs = B * n;
+        for (uint32_t i = lane; i < npairs; i += 32) {
+            uint32_t g = i / n, p = i - g * n;
+            uint32_t prov = ws.prov[g];
+            const uint32_t *cl = ws.cl0 + g * n;
+            uint32_t cp = (prov >> p & 1u) ? cl[p] : (cl[p] & ~(1u << p));
+            uint32_t closure = cp, todo = cp, valid = 0;
+            while (todo) {
+                uint32_t q = __ffs(todo) - 1;
+                todo &= ~(1u << q);
+                uint32_t cq = (prov >> q & 1u) ? cl[q] : (cl[q] & ~(1u << q));
+                valid |= (cq >> q) & 1u;
+                todo |= cq & ~closure & ~(1u << q);
+                closure |= cq;
+            }
+            ws.clo[i] = closure;
+            if (valid && closure) atomicMin(&ws.best[g], ((uint32_t)__popc(closure) << 5) | p);
+        }
+        __syncwarp();
+        if (lane < B) {
+            uint32_t b = ws.best[lane];
+            uint32_t all = (n == 32) ? kFull : ((1u << n) - 1u);
+            ws.sel[lane] = (b == kFull || (b >> 5) >= n) ? all : ws.clo[lane * n + (b & 31u)];
+        }
+        __syncwarp();
+    }
+
+    __device__ void emit(uint32_t B, bool decide) {
+        const uint32_t n = M.n;
+        const uint32_t npairs = B * n;
+        const bool filter = (MODE != MODE_PLAIN) && !decide;
+        uint32_t pair = lane;
+        int stage = 0;
+        uint32_t g = 0, p = 0, j = 0, lcnt = 0, loff = 0, arem = 0, roff = 0;
+        uint32_t rmask = 0, ract = 0, pidx = 0, psize = 0;
+        K key;
+        memset(&key, 0, sizeof key);
+        uint32_t head = 0, count = 0;
+        for (;;) {
+            bool have = false;
+            K out;
+            uint32_t omask = 0;
+            while (!have && stage != 3) {
+                if (stage == 0) {
+                    if (pair >= npairs) {
+                        stage = 3;
+                        break;
+                    }
+                    g = pair / n;
+                    p = pair - g * n;
+                    key = ws.keys[g];
+                    uint32_t s = KT<K>::get(key, M.fb(p), M.bs(p));
+                    const uint32_t *rec = M.rec(p, s);
+                    uint32_t sel = filter ? ws.sel[g] : kFull;
+                    lcnt = (sel >> p & 1u) ? rec[R_LCNT] : 0u;
+                    loff = rec[R_LOFF];
+                    roff = rec[R_ROFF];
+                    arem = ws.appl[pair];
+                    if (filter) {
+                        uint32_t a = arem;
+                        while (a) {
+                            uint32_t r = __ffs(a) - 1;
+                            a &= a - 1;
+                            uint32_t m = M.rmask(M.lrule(roff + r));
+                            if ((m & sel) != m) arem &= ~(1u << r);
+                        }
+                    }
+                    j = 0;
+                    pidx = psize = 0;
+                    stage = 1;
+                }
+                if (stage == 1) {
+                    if (j < lcnt) {
+                        out = key;
+                        KT<K>::set(out, M.fb(p), M.bs(p), M.ltgt(loff + j));
+                        j++;
+                        omask = 1u << p;
+                        have = true;
+                        break;
+                    }
+                    stage = 2;
+                }
+                if (stage == 2) {
+                    if (pidx < psize) {
+                        out = key;
+                        uint32_t idx = pidx, rest = rmask;
+                        while (rest) {
+                            uint32_t q = __ffs(rest) - 1;
+                            rest &= rest - 1;
+                            uint32_t sq = KT<K>::get(key, M.fb(q), M.bs(q));
+                            const uint32_t *grp = M.group(M.rec(q, sq), ract);
+                            uint32_t tc = grp[2];
+                            uint32_t d = idx % tc;
+                            idx /= tc;
+                            KT<K>::set(out, M.fb(q), M.bs(q), M.stgt(grp[1] + d));
+                        }
+                        pidx++;
+                        omask = rmask;
+                        have = true;
+                        break;
+                    }
+                    if (arem == 0) {
+                        stage = 0;
+                        pair += 32;
+                        continue;
+                    }
+                    uint32_t r = __ffs(arem) - 1;
+                    arem &= arem - 1;
+                    uint32_t k = M.lrule(roff + r);
+                    rmask = M.rmask(k);
+                    ract = M.ract(k);
+                    psize = 1;
+                    uint32_t rest = rmask;
+                    while (rest) {
+                        uint32_t q = __ffs(rest) - 1;
+                        rest &= rest - 1;
+                        uint32_t sq = KT<K>::get(key, M.fb(q), M.bs(q));
+                        psize *= M.group(M.rec(q, sq), ract)[2];
+                    }
+                    pidx = 0;
+                }
+            }
+            uint32_t bal = __ballot_sync(kFull, have);
+            if (!bal) break;
+            if (have) {
+                uint32_t pos = (head + count + __popc(bal & lanemask_lt)) % kQcap;
+                ws.qkey[pos] = out;
+                ws.qg[pos] = g;
+                ws.qmask[pos] = omask;
+            }
+            count += __popc(bal);
+            __syncwarp();
+            if (count >= 32) {
+                drain(head, 32, decide);
+                head = (head + 32) % kQcap;
+                count -= 32;
+                __syncwarp();
+            }
+        }
+        if (count) {
+            drain(head, count, decide);
+            __syncwarp();
+        }
+    }
+
+    __device__ void flush_stats() {
+        Ctrl *c = P.ctrl;
+        unsigned int v[5] = {st.lookups, st.probes, st.inserts, st.expanded, st.ilookups};
+#pragma unroll
+        for (int k = 0; k < 5; k++)
+            for (int o = 16; o; o >>= 1) v[k] += __shfl_xor_sync(kFull, v[k], o);
+        unsigned int viol = __any_sync(kFull, st.violation);
+        if (lane == 0) {
+            if (v[0]) atomicAdd(&c->lookups, (unsigned long long)v[0]);
+            if (v[1]) atomicAdd(&c->probes, (unsigned long long)v[1]);
+            if (v[2]) atomicAdd(&c->inserts, (unsigned long long)v[2]);
+            if (v[3]) atomicAdd(&c->expanded, (unsigned long long)v[3]);
+            if (v[4]) atomicAdd(&c->inserts_lookups, (unsigned long long)v[4]);
+            if (viol) atomicOr(&c->violation, 1u);
+        }
+        st = WarpStats{0, 0, 0, 0, 0, 0};
+    }
+};
+
+template <class K, int MODE> __global__ void __launch_bounds__(256) explore_kernel(Params P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t *model = P.model;
+    size_t model_bytes = 0;
+    if (P.model_in_smem) {
+        uint32_t *m = (uint32_t *)smem;
+        for (uint32_t i = threadIdx.x; i < P.model_words; i += blockDim.x) m[i] = __ldg(P.model + i);
+        model = m;
+        model_bytes = ((size_t)P.model_words * 4 + 127) & ~(size_t)127;
+    }
+    WarpScratch<K> *wsall = (WarpScratch<K> *)(smem + model_bytes);
+    WarpScratch<K> &ws = wsall[threadIdx.x >> 5];
+    __syncthreads();
+
+    Explorer<K, MODE> E(P, model, ws);
+    Ctrl *c = P.ctrl;
+    const uint32_t n = E.M.n;
+    uint32_t B = kPairMax / n;
+    if (B > 32) B = 32;
+    if (B < 1) B = 1;
+    for (;;) {
+        unsigned long long lo = vload(&c->lo), hi = vload(&c->hi);
+        unsigned int claim = vload(&c->claim);
+        bool decide = (MODE == MODE_PROVISO) && vload(&c->phase) == PH_DECIDE;
+        unsigned long long nlev = hi - lo;
+        for (;;) {
+            unsigned long long base = 0;
+            if (E.lane == 0) base = atomicAdd(&c->cursor, (unsigned long long)claim);
+            base = __shfl_sync(kFull, base, 0);
+            if (base >= nlev || vload(&c->error)) break;
+            unsigned long long end = base + claim < nlev ? base + claim : nlev;
+            for (unsigned long long b = base; b < end; b += B) {
+                uint32_t cnt = (uint32_t)((end - b) < B ? (end - b) : B);
+                E.batch(lo + b, cnt, b, decide);
+            }
+        }
+        E.flush_stats();
+        grid_barrier<MODE>(P);
+        if (vload(&c->done) || vload(&c->pause) || vload(&c->error)) break;
+    }
+}
+
+// Insert the all-zero initial state (GPUexplore.cu:668-682).
+template <class K> __global__ void init_kernel(Params P) {
+    if (threadIdx.x != 0) return;
+    K key = KT<K>::initial();
+    unsigned int probes = 0;
+    find_or_insert<K>((K *)P.table, P.nbuckets, key, KT<K>::hash(key, P.seed), probes);
+    ((K *)P.store)[0] = key;
+    P.levels[0] = 1;
+}
+
+// Order-independent hash of the visited set over the state-vector words
+// (the sum of per-state key hashes; the oracle computes the same sum).
+template <class K>
+__global__ void set_hash_kernel(const K *store, unsigned long long count, uint32_t words,
+                                unsigned long long *out) {
+    unsigned long long acc = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < count;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t w[4];
+        KT<K>::words(KT<K>::load(store + i), w);
+        uint64_t h = 0x9E3779B97F4A7C15ull;
+        for (uint32_t j = 0; j < words; j += 2) {
+            uint64_t cc = w[j];
+            if (j + 1 < words) cc |= (uint64_t)w[j + 1] << 32;
+            h = mix64(h ^ cc);
+        }
+        acc += h;
+    }
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
+// Occupied slots of the table (count_states, GPUexplore.cu:687-704).
+template <class K> __global__ void count_kernel(const K *table, unsigned long long slots, unsigned long long *out) {
+    unsigned long long acc = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        K k = KT<K>::load(table + i);
+        acc += KT<K>::empty(k) ? 0 : 1;
+    }
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
+// Convert store keys to state-vector words on the device (for collection).
+template <class K>
+__global__ void words_kernel(const K *store, unsigned long long count, uint32_t words, uint32_t *out) {
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < count;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t w[4];
+        KT<K>::words(KT<K>::load(store + i), w);
+        for (uint32_t j = 0; j < words; j++) out[i * words + j] = w[j];
+    }
+}
+
+} // namespace gpx
+
+// ========================================================================= host
+
+using namespace gpx;
+
+namespace {
+
+const char *kStatusStrings[] = {"ok",
+                                "input network does not exist or is malformed",
+                                "no CUDA compatible GPU detected",
+                                "CUDA runtime error",
+                                "problem with hash table",
+                                "device-side wait timed out",
+                                "invalid argument",
+                                "model outside the supported limits",
+                                "state store full",
+                                "out of memory"};
+
+struct KernelSet {
+    void (*explore[3])(Params);
+    void (*init)(Params);
+    size_t scratch_bytes;
+    uint32_t slot_bytes, bucket_slots;
+};
+
+template <class K> KernelSet kernels_for() {
+    KernelSet s;
+    s.explore[0] = explore_kernel<K, MODE_PLAIN>;
+    s.explore[1] = explore_kernel<K, MODE_POR>;
+    s.explore[2] = explore_kernel<K, MODE_PROVISO>;
+    s.init = init_kernel<K>;
+    s.scratch_bytes = sizeof(WarpScratch<K>);
+    s.slot_bytes = sizeof(K);
+    s.bucket_slots = KT<K>::kSlots;
+    return s;
+}
+
+#define GPX_CUDA(call)                                                                                        \
+    do {                                                                                                      \
+        cudaError_t _e = (call);                                                                              \
+        if (_e != cudaSuccess) {                                                                              \
+            fprintf(stderr, "gpx: %s failed: %s\n", #call, cudaGetErrorString(_e));                         \
+            return (_e == cudaErrorMemoryAllocation) ? GPX_ERR_NOMEM : GPX_ERR_CUDA;                          \
+        }                                                                                                     \
+    } while (0)
+
+} // namespace
+
+struct gpx_explorer {
+    gpx_options o;
+    gpx_model model;
+    int kind = 0; // 0: 32-bit, 1: 64-bit, 2: 128-bit slots
+    KernelSet ks;
+    int mode = MODE_PLAIN;
+    int property = GPX_PROP_NONE;
+    cudaDeviceProp prop;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    void *d_table = nullptr;
+    unsigned long long nbuckets = 0, slots = 0;
+    size_t table_bytes = 0;
+    void *d_store = nullptr;
+    unsigned long long store_cap = 0;
+    uint32_t *d_model = nullptr;
+    size_t model_cap_words = 0;
+    uint32_t *d_sel = nullptr;
+    unsigned long long *d_levels = nullptr;
+    unsigned long long *d_scalar = nullptr;
+    Ctrl *d_ctrl = nullptr;
+    Ctrl *h_ctrl = nullptr;
+    int blocks = 0, threads = 0;
+    size_t smem = 0;
+    bool model_in_smem = false;
+    unsigned long long last_count = 0, last_lo = 0, last_hi = 0;
+    uint32_t bits_statevector = 0;
+};
+
+namespace {
+
+int select_kind(uint32_t state_bits) {
+    if (state_bits <= 31) return 0;
+    if (state_bits <= 63) return 1;
+    return 2;
+}
+
+int load_text(const std::string &path, gpx_model **out) {
+    std::ifstream f(path);
+    if (!f) return GPX_ERR_PARSE;
+    std::stringstream ss;
+    ss << f.rdbuf();
+    gpx_model *m = new gpx_model;
+    std::string err = parse_gpf_text(ss.str(), &m->gpf);
+    if (err.empty()) err = decode_gpf(m->gpf, &m->dec);
+    if (!err.empty()) {
+        fprintf(stderr, "gpx: %s: %s\n", path.c_str(), err.c_str());
+        int code = err.rfind("UNSUPPORTED", 0) == 0 ? GPX_ERR_UNSUPPORTED : GPX_ERR_PARSE;
+        delete m;
+        return code;
+    }
+    *out = m;
+    return GPX_OK;
+}
+
+int configure_launch(gpx_explorer *ex) {
+    const size_t model_bytes = ex->model.dec.words.size() * 4;
+    int threads = ex->o.threads > 0 ? ex->o.threads : 256;
+    if (threads % 32 || threads > 256) return GPX_ERR_INVALID;
+    const size_t smem_limit = ex->prop.sharedMemPerBlockOptin;
+    size_t scratch = (size_t)(threads / 32) * ex->ks.scratch_bytes;
+    size_t mb = (model_bytes + 127) & ~(size_t)127;
+    ex->model_in_smem = (mb + scratch <= smem_limit) && model_bytes <= 96 * 1024;
+    ex->smem = scratch + (ex->model_in_smem ? mb : 0);
+    if (ex->smem > smem_limit) return GPX_ERR_UNSUPPORTED;
+    for (int md = 0; md < 3; md++)
+        GPX_CUDA(cudaFuncSetAttribute((const void *)ex->ks.explore[md], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)ex->smem));
+    int per_sm = 0;
+    GPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)ex->ks.explore[ex->mode],
+                                                           threads, ex->smem));
+    if (per_sm < 1) return GPX_ERR_UNSUPPORTED;
+    int max_blocks = per_sm * ex->prop.multiProcessorCount;
+    int blocks = ex->o.blocks > 0 ? std::min(ex->o.blocks, max_blocks) : max_blocks;
+    ex->blocks = std::max(1, blocks);
+    ex->threads = threads;
+    return GPX_OK;
+}
+
+int upload_model(gpx_explorer *ex) {
+    const std::vector<uint32_t> &w = ex->model.dec.words;
+    if (w.size() > ex->model_cap_words) {
+        if (ex->d_model) cudaFree(ex->d_model);
+        ex->d_model = nullptr;
+        GPX_CUDA(cudaMalloc(&ex->d_model, w.size() * 4));
+        ex->model_cap_words = w.size();
+    }
+    GPX_CUDA(cudaMemcpyAsync(ex->d_model, w.data(), w.size() * 4, cudaMemcpyHostToDevice, ex->st));
+    return GPX_OK;
+}
+
+Params make_params(gpx_explorer *ex) {
+    Params P;
+    memset(&P, 0, sizeof P);
+    P.table = ex->d_table;
+    P.nbuckets = ex->nbuckets;
+    P.store = ex->d_store;
+    P.store_cap = ex->store_cap;
+    P.model = ex->d_model;
+    P.model_words = (uint32_t)ex->model.dec.words.size();
+    P.model_in_smem = ex->model_in_smem;
+    P.sel = ex->d_sel;
+    P.levels = ex->d_levels;
+    P.ctrl = ex->d_ctrl;
+    P.seed = ex->o.seed;
+    P.max_states = ex->o.max_states;
+    P.timeout_ns = 20ull * 1000 * 1000 * 1000;
+    P.property = (uint32_t)ex->property;
+    P.levels_per_launch = ex->o.kernel_iters > 0 ? (uint32_t)ex->o.kernel_iters : 0;
+    P.total_warps = (uint32_t)(ex->blocks * (ex->threads / 32));
+    return P;
+}
+
+void print_states(FILE *out, gpx_explorer *ex, const std::vector<uint32_t> &words, unsigned long long count,
+                  unsigned long long unexplored_from) {
+    const Gpf &g = ex->model.gpf;
+    const uint32_t W = ex->model.dec.key_words;
+    const uint32_t sv = (ex->bits_statevector + 31) / 32;
+    unsigned long long newcount = 0;
+    for (unsigned long long i = 0; i < count; i++) {
+        const uint32_t *v = words.data() + i * W;
+        if (i >= unexplored_from) {
+            fprintf(out, "new: ");
+            newcount++;
+        }
+        for (uint32_t p = 0; p < g.nr_procs; p++) {
+            uint32_t lo = g.firstbit[p], w = g.bits_state[p];
+            uint64_t x = v[lo / 32];
+            if ((lo % 32) + w > 32) x |= (uint64_t)v[lo / 32 + 1] << 32;
+            fprintf(out, "%u%s", (uint32_t)((x >> (lo % 32)) & ((1ull << w) - 1)), p + 1 < g.nr_procs ? "," : "");
+        }
+        fprintf(out, " ");
+        for (uint32_t j = 0; j < sv; j++) fprintf(out, "%d ", (int)(j < W ? v[j] : 0u));
+        fprintf(out, "\n");
+    }
+    fprintf(out, "nr. of states in hash table: %llu (%llu unexplored states)\n", count, newcount);
+}
+
+int collect_words(gpx_explorer *ex, unsigned long long count, std::vector<uint32_t> *out) {
+    const uint32_t W = ex->model.dec.key_words;
+    out->assign(count * W, 0);
+    if (!count) return GPX_OK;
+    uint32_t *d_words = nullptr;
+    GPX_CUDA(cudaMalloc(&d_words, count * W * 4));
+    int blocks = (int)std::min<unsigned long long>((count + 255) / 256, 4096);
+    if (ex->kind == 0)
+        words_kernel<K32><<<blocks, 256, 0, ex->st>>>((const K32 *)ex->d_store, count, W, d_words);
+    else if (ex->kind == 1)
+        words_kernel<K64><<<blocks, 256, 0, ex->st>>>((const K64 *)ex->d_store, count, W, d_words);
+    else
+        words_kernel<K128><<<blocks, 256, 0, ex->st>>>((const K128 *)ex->d_store, count, W, d_words);
+    cudaError_t e = cudaMemcpyAsync(out->data(), d_words, count * W * 4, cudaMemcpyDeviceToHost, ex->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ex->st);
+    cudaFree(d_words);
+    if (e != cudaSuccess) return GPX_ERR_CUDA;
+    return GPX_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *gpx_status_string(int status) {
+    if (status < 0 || status > GPX_ERR_NOMEM) return "unknown status";
+    return kStatusStrings[status];
+}
+
+int gpx_abi_version(void) { return GPX_ABI_VERSION; }
+
+int gpx_device_info_get(int device, gpx_device_info *info) {
+    if (!info) return GPX_ERR_INVALID;
+    memset(info, 0, sizeof *info);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPX_ERR_NO_GPU;
+    if (device < 0 || device >= ndev) return GPX_ERR_INVALID;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return GPX_ERR_CUDA;
+    info->total_global_mem = prop.totalGlobalMem;
+    info->shared_mem_per_block = (int32_t)prop.sharedMemPerBlock;
+    info->shared_mem_per_sm = (int32_t)prop.sharedMemPerMultiprocessor;
+    info->max_threads_per_block = prop.maxThreadsPerBlock;
+    info->max_grid_size = prop.maxGridSize[0];
+    info->sm_count = prop.multiProcessorCount;
+    snprintf(info->name, sizeof info->name, "%s", prop.name);
+    return GPX_OK;
+}
+
+void gpx_options_init(gpx_options *o) {
+    memset(o, 0, sizeof *o);
+    o->struct_size = sizeof *o;
+    o->seed = 0x243F6A8885A308D3ull;
+}
+
+int gpx_model_load(const char *path_without_ext, gpx_model **out) {
+    if (!path_without_ext || !out) return GPX_ERR_INVALID;
+    return load_text(std::string(path_without_ext) + ".gpf", out);
+}
+
+int gpx_model_load_file(const char *path, gpx_model **out) {
+    if (!path || !out) return GPX_ERR_INVALID;
+    return load_text(path, out);
+}
+
+int gpx_model_from_words(const uint32_t *words, size_t nwords, gpx_model **out) {
+    if (!words || !out) return GPX_ERR_INVALID;
+    gpx_model *m = new gpx_model;
+    std::string err = parse_gpf_words(words, nwords, &m->gpf);
+    if (err.empty()) err = decode_gpf(m->gpf, &m->dec);
+    if (!err.empty()) {
+        int code = err.rfind("UNSUPPORTED", 0) == 0 ? GPX_ERR_UNSUPPORTED : GPX_ERR_PARSE;
+        delete m;
+        return code;
+    }
+    *out = m;
+    return GPX_OK;
+}
+
+int gpx_model_info_get(const gpx_model *m, gpx_model_info *info) {
+    if (!m || !info) return GPX_ERR_INVALID;
+    memset(info, 0, sizeof *info);
+    const Gpf &g = m->gpf;
+    info->liveness = g.liveness;
+    info->nr_procs = g.nr_procs;
+    info->bits_act = g.bits_act;
+    info->proc_nrstates = g.proc_nrstates;
+    info->bits_statevector = g.bits_statevector;
+    info->nbits_offset = g.nbits_offset;
+    info->max_buf_ints = g.max_buf_ints;
+    info->nr_trans = g.nr_trans;
+    info->state_bits = m->dec.state_bits;
+    info->key_words = m->dec.key_words;
+    for (uint32_t p = 0; p <= g.nr_procs; p++) info->firstbit[p] = g.firstbit[p];
+    for (uint32_t p = 0; p < g.nr_procs; p++) info->bits_state[p] = g.bits_state[p];
+    return GPX_OK;
+}
+
+void gpx_model_free(gpx_model *m) { delete m; }
+
+void gpx_explorer_destroy(gpx_explorer *ex) {
+    if (!ex) return;
+    if (ex->d_table) cudaFree(ex->d_table);
+    if (ex->d_store) cudaFree(ex->d_store);
+    if (ex->d_model) cudaFree(ex->d_model);
+    if (ex->d_sel) cudaFree(ex->d_sel);
+    if (ex->d_levels) cudaFree(ex->d_levels);
+    if (ex->d_scalar) cudaFree(ex->d_scalar);
+    if (ex->d_ctrl) cudaFree(ex->d_ctrl);
+    if (ex->h_ctrl) cudaFreeHost(ex->h_ctrl);
+    for (auto &e : ex->ev)
+        if (e) cudaEventDestroy(e);
+    if (ex->st) cudaStreamDestroy(ex->st);
+    delete ex;
+}
+
+int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_explorer **out) {
+    if (!model || !opts || !out || opts->struct_size != sizeof(gpx_options)) return GPX_ERR_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPX_ERR_NO_GPU;
+    if (opts->device < 0 || opts->device >= ndev) return GPX_ERR_INVALID;
+    gpx_explorer *ex = new gpx_explorer;
+    ex->o = *opts;
+    ex->model = *model;
+    ex->property = opts->property;
+    if (ex->property == GPX_PROP_SAFETY && model->gpf.liveness == 1) ex->property = GPX_PROP_LIVENESS;
+    ex->mode = opts->por ? (opts->cycle_proviso ? MODE_PROVISO : MODE_POR) : MODE_PLAIN;
+    ex->kind = select_kind(model->dec.state_bits);
+    ex->ks = ex->kind == 0 ? kernels_for<K32>() : (ex->kind == 1 ? kernels_for<K64>() : kernels_for<K128>());
+    ex->bits_statevector = model->gpf.bits_statevector + (opts->por ? 1u : 0u);
+    int rc = GPX_OK;
+    auto fail = [&](int code) {
+        gpx_explorer_destroy(ex);
+        return code;
+    };
+    if (cudaSetDevice(opts->device) != cudaSuccess) return fail(GPX_ERR_CUDA);
+    if (cudaGetDeviceProperties(&ex->prop, opts->device) != cudaSuccess) return fail(GPX_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&ex->st, cudaStreamNonBlocking) != cudaSuccess) return fail(GPX_ERR_CUDA);
+    for (auto &e : ex->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return fail(GPX_ERR_CUDA);
+    if ((rc = configure_launch(ex)) != GPX_OK) return fail(rc);
+
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return fail(GPX_ERR_CUDA);
+    const size_t bucket_bytes = (size_t)ex->ks.slot_bytes * ex->ks.bucket_slots;
+    size_t tb = opts->q_words ? (size_t)opts->q_words * 4 : free_b / 4;
+    tb = (tb / bucket_bytes) * bucket_bytes;
+    if (tb < bucket_bytes) return fail(GPX_ERR_INVALID);
+    ex->table_bytes = tb;
+    ex->nbuckets = tb / bucket_bytes;
+    ex->slots = ex->nbuckets * ex->ks.bucket_slots;
+    const size_t per_state = ex->ks.slot_bytes + (ex->mode == MODE_PROVISO ? 4 : 0);
+    unsigned long long cap = opts->store_states ? opts->store_states : ex->slots;
+    size_t margin = (size_t)512 << 20;
+    size_t avail = free_b > tb + margin ? free_b - tb - margin : 0;
+    if (!opts->store_states && cap * per_state > avail) cap = avail / per_state;
+    if (cap < 1) return fail(GPX_ERR_NOMEM);
+    ex->store_cap = cap;
+    if (cudaMalloc(&ex->d_table, tb) != cudaSuccess) return fail(GPX_ERR_NOMEM);
+    if (cudaMalloc(&ex->d_store, cap * ex->ks.slot_bytes) != cudaSuccess) return fail(GPX_ERR_NOMEM);
+    if (ex->mode == MODE_PROVISO && cudaMalloc(&ex->d_sel, cap * 4) != cudaSuccess) return fail(GPX_ERR_NOMEM);
+    if (cudaMalloc(&ex->d_levels, (size_t)kMaxLevels * 8) != cudaSuccess) return fail(GPX_ERR_NOMEM);
+    if (cudaMalloc(&ex->d_scalar, 64) != cudaSuccess) return fail(GPX_ERR_NOMEM);
+    if (cudaMalloc(&ex->d_ctrl, sizeof(Ctrl)) != cudaSuccess) return fail(GPX_ERR_NOMEM);
+    if (cudaMallocHost(&ex->h_ctrl, sizeof(Ctrl)) != cudaSuccess) return fail(GPX_ERR_NOMEM);
+    if ((rc = upload_model(ex)) != GPX_OK) return fail(rc);
+    if (cudaStreamSynchronize(ex->st) != cudaSuccess) return fail(GPX_ERR_CUDA);
+    *out = ex;
+    return GPX_OK;
+}
+
+int gpx_explorer_set_model(gpx_explorer *ex, const gpx_model *model) {
+    if (!ex || !model) return GPX_ERR_INVALID;
+    if (select_kind(model->dec.state_bits) != ex->kind) return GPX_ERR_INVALID;
+    ex->model = *model;
+    ex->bits_statevector = model->gpf.bits_statevector + (ex->o.por ? 1u : 0u);
+    int rc = configure_launch(ex);
+    if (rc != GPX_OK) return rc;
+    return upload_model(ex);
+}
+
+int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
+    if (!ex || !r) return GPX_ERR_INVALID;
+    memset(r, 0, sizeof *r);
+    r->struct_size = sizeof *r;
+    if (cudaSetDevice(ex->o.device) != cudaSuccess) return GPX_ERR_CUDA;
+    Params P = make_params(ex);
+    // reset: empty table, empty store, initial state (GPUexplore.cu:2091-2092)
+    GPX_CUDA(cudaEventRecord(ex->ev[0], ex->st));
+    GPX_CUDA(cudaMemsetAsync(ex->d_table, 0, ex->table_bytes, ex->st));
+    Ctrl c0;
+    memset(&c0, 0, sizeof c0);
+    c0.store_count = 1;
+    c0.lo = 0;
+    c0.hi = 1;
+    c0.nlevels = 1;
+    c0.claim = 32;
+    c0.phase = ex->mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND;
+    *ex->h_ctrl = c0;
+    GPX_CUDA(cudaMemcpyAsync(ex->d_ctrl, ex->h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, ex->st));
+    ex->ks.init<<<1, 32, 0, ex->st>>>(P);
+    GPX_CUDA(cudaGetLastError());
+    GPX_CUDA(cudaEventRecord(ex->ev[1], ex->st));
+    void (*kern)(Params) = ex->ks.explore[ex->mode];
+    void *args[] = {&P};
+    unsigned long long launches = 0;
+    float kernel_ms = 0;
+    for (;;) {
+        GPX_CUDA(cudaEventRecord(ex->ev[2], ex->st));
+        GPX_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(ex->blocks), dim3(ex->threads), args, ex->smem,
+                                             ex->st));
+        GPX_CUDA(cudaEventRecord(ex->ev[3], ex->st));
+        launches++;
+        GPX_CUDA(cudaMemcpyAsync(ex->h_ctrl, ex->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, ex->st));
+        GPX_CUDA(cudaStreamSynchronize(ex->st));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ex->ev[2], ex->ev[3]);
+        kernel_ms += ms;
+        Ctrl &c = *ex->h_ctrl;
+        if (ex->o.verbosity == 1) printf("%llu\n", launches - 1);
+        if (ex->o.verbosity >= 2) {
+            unsigned long long cnt = std::min<unsigned long long>(c.store_count, ex->store_cap);
+            if (ex->o.verbosity == 2) {
+                printf("nr. of states in hash table: %llu (%llu unexplored states)\n", cnt, cnt - c.lo);
+            } else {
+                std::vector<uint32_t> w;
+                int rc = collect_words(ex, cnt, &w);
+                if (rc != GPX_OK) return rc;
+                print_states(stdout, ex, w, cnt, c.lo);
+            }
+        }
+        if (c.done || c.error) break;
+        // -k budget reached: resume with a fresh launch
+        c.pause = 0;
+        c.launch_levels = 0;
+        GPX_CUDA(cudaMemcpyAsync(&ex->d_ctrl->pause, &c.pause, sizeof(unsigned int), cudaMemcpyHostToDevice, ex->st));
+        GPX_CUDA(cudaMemcpyAsync(&ex->d_ctrl->launch_levels, &c.launch_levels, sizeof(unsigned int),
+                                 cudaMemcpyHostToDevice, ex->st));
+    }
+    Ctrl &c = *ex->h_ctrl;
+    float setup_ms = 0, total_ms = 0;
+    cudaEventElapsedTime(&setup_ms, ex->ev[0], ex->ev[1]);
+    cudaEventElapsedTime(&total_ms, ex->ev[1], ex->ev[3]);
+    r->status = c.error ? (int)c.error : GPX_OK;
+    r->stopped = (int)c.stop;
+    if (c.error) r->stopped = GPX_STOP_ERROR;
+    r->verdict = (c.stop == GPX_STOP_VIOLATION) ? ex->property : GPX_PROP_NONE;
+    unsigned long long count = std::min<unsigned long long>(c.store_count, ex->store_cap);
+    r->states = count;
+    r->nlevels = c.nlevels;
+    r->level_counts = (uint64_t *)malloc(sizeof(uint64_t) * std::max(1u, c.nlevels));
+    GPX_CUDA(cudaMemcpyAsync(r->level_counts, ex->d_levels, sizeof(uint64_t) * c.nlevels, cudaMemcpyDeviceToHost,
+                             ex->st));
+    r->lookups = c.lookups;
+    r->transitions = c.inserts_lookups; // successors sent to the table for insertion
+    r->probes = c.probes;
+    r->expanded = c.expanded;
+    r->launches = launches;
+    r->kernel_ms = kernel_ms;
+    r->explore_ms = total_ms;
+    r->setup_ms = setup_ms;
+    r->key_words = ex->model.dec.key_words;
+    r->table_slots = ex->slots;
+    r->slot_bytes = ex->ks.slot_bytes;
+    r->blocks = (uint32_t)ex->blocks;
+    r->threads = (uint32_t)ex->threads;
+    // set hash over the visited states
+    GPX_CUDA(cudaMemsetAsync(ex->d_scalar, 0, 16, ex->st));
+    {
+        int blocks = (int)std::min<unsigned long long>((count + 255) / 256, 4096);
+        blocks = std::max(blocks, 1);
+        if (ex->kind == 0)
+            set_hash_kernel<K32><<<blocks, 256, 0, ex->st>>>((const K32 *)ex->d_store, count, r->key_words,
+                                                             ex->d_scalar);
+        else if (ex->kind == 1)
+            set_hash_kernel<K64><<<blocks, 256, 0, ex->st>>>((const K64 *)ex->d_store, count, r->key_words,
+                                                             ex->d_scalar);
+        else
+            set_hash_kernel<K128><<<blocks, 256, 0, ex->st>>>((const K128 *)ex->d_store, count, r->key_words,
+                                                              ex->d_scalar);
+        if (ex->o.collect_states || ex->o.verbosity >= 2) {
+            int cb = (int)std::min<unsigned long long>((ex->slots + 255) / 256, 8192);
+            if (ex->kind == 0)
+                count_kernel<K32><<<cb, 256, 0, ex->st>>>((const K32 *)ex->d_table, ex->slots, ex->d_scalar + 1);
+            else if (ex->kind == 1)
+                count_kernel<K64><<<cb, 256, 0, ex->st>>>((const K64 *)ex->d_table, ex->slots, ex->d_scalar + 1);
+            else
+                count_kernel<K128><<<cb, 256, 0, ex->st>>>((const K128 *)ex->d_table, ex->slots, ex->d_scalar + 1);
+        }
+        GPX_CUDA(cudaGetLastError());
+        unsigned long long h[2] = {0, 0};
+        GPX_CUDA(cudaMemcpyAsync(h, ex->d_scalar, 16, cudaMemcpyDeviceToHost, ex->st));
+        GPX_CUDA(cudaStreamSynchronize(ex->st));
+        r->set_hash = h[0];
+        r->table_count = h[1];
+    }
+    if (ex->o.collect_states) {
+        std::vector<uint32_t> w;
+        int rc = collect_words(ex, count, &w);
+        if (rc != GPX_OK) return rc;
+        r->states_buf = (uint32_t *)malloc(std::max<size_t>(w.size(), 1) * 4);
+        memcpy(r->states_buf, w.data(), w.size() * 4);
+    }
+    ex->last_count = count;
+    ex->last_lo = c.lo;
+    ex->last_hi = c.hi;
+    return r->status;
+}
+
+int gpx_explore(const gpx_model *model, const gpx_options *opts, gpx_result *result) {
+    if (!result) return GPX_ERR_INVALID;
+    memset(result, 0, sizeof *result);
+    result->struct_size = sizeof *result;
+    gpx_explorer *ex = nullptr;
+    int rc = gpx_explorer_create(model, opts, &ex);
+    if (rc != GPX_OK) {
+        result->status = rc;
+        result->stopped = GPX_STOP_ERROR;
+        return rc;
+    }
+    rc = gpx_explorer_run(ex, result);
+    gpx_explorer_destroy(ex);
+    return rc;
+}
+
+void gpx_result_free(gpx_result *r) {
+    if (!r) return;
+    free(r->level_counts);
+    free(r->states_buf);
+    r->level_counts = nullptr;
+    r->states_buf = nullptr;
+}
+
+int gpx_explorer_dump(gpx_explorer *ex, const char *path) {
+    if (!ex || !path) return GPX_ERR_INVALID;
+    FILE *f = fopen(path, "w");
+    if (!f) return GPX_ERR_INVALID;
+    std::vector<uint32_t> w;
+    int rc = collect_words(ex, ex->last_count, &w);
+    if (rc == GPX_OK) {
+        // the level that would have been expanded next, [lo, count), is unexplored
+        unsigned long long unexplored_from = std::min(ex->last_lo, ex->last_count);
+        if (ex->h_ctrl->stop == GPX_STOP_DONE) unexplored_from = ex->last_count;
+        print_states(f, ex, w, ex->last_count, unexplored_from);
+    }
+    fclose(f);
+    return rc;
+}
+
+} // extern "C"

@@ -1,0 +1,276 @@
+// gpx_model.cpp -- gpf parsing (GPUexplore.cu:1885-1987) and decoding into the
+// flat device layout described in gpx_model.h.
+#include "gpx_model.h"
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <set>
+
+namespace gpx {
+
+namespace {
+
+struct Cursor {
+    const uint32_t *w;
+    size_t n, i = 0;
+    bool ok = true;
+    uint32_t next() {
+        if (i >= n) {
+            ok = false;
+            return 0;
+        }
+        return w[i++];
+    }
+    std::vector<uint32_t> take(uint64_t count) {
+        std::vector<uint32_t> v;
+        if (count > n - std::min(n, i)) {
+            ok = false;
+            return v;
+        }
+        v.assign(w + i, w + i + count);
+        i += count;
+        return v;
+    }
+};
+
+uint32_t packed_field(const uint32_t *words, uint32_t i, uint32_t nbits) {
+    uint32_t per = 32 / nbits;
+    return (words[i / per] >> ((i % per) * nbits)) & ((1u << nbits) - 1u);
+}
+
+} // namespace
+
+std::string parse_gpf_words(const uint32_t *w, size_t n, Gpf *g) {
+    Cursor c{w, n};
+    *g = Gpf();
+    // field order of GPUexplore.cu:1888-1982
+    g->liveness = c.next();
+    g->nr_procs = c.next();
+    g->bits_act = c.next();
+    g->proc_nrstates = c.next();
+    g->bits_statevector = c.next();
+    if (!c.ok) return "truncated header";
+    if (g->nr_procs < 1 || g->nr_procs > (uint32_t)kMaxProcs) return "nr_procs outside 1..31";
+    g->firstbit = c.take(g->nr_procs + 1);
+    g->bits_state = c.take(g->nr_procs);
+    g->nbits_offset = c.next();
+    g->max_buf_ints = c.next();
+    g->proc_offsets_start = c.take(g->nr_procs + 1);
+    if (!c.ok) return "truncated process layout";
+    g->proc_offsets = c.take(g->proc_offsets_start[g->nr_procs]);
+    g->nr_trans = c.next();
+    if (!c.ok) return "truncated offsets";
+    g->proc_trans = c.take(g->nr_trans);
+    g->nbits_syncbits_offset = c.next();
+    g->nr_syncbits_offsets = c.next();
+    if (!c.ok) return "truncated transitions";
+    g->syncbits_offsets = c.take(g->nr_syncbits_offsets);
+    g->nr_syncbits = c.next();
+    if (!c.ok) return "truncated synchronisation offsets";
+    g->syncbits = c.take(g->nr_syncbits);
+    if (!c.ok) return "truncated synchronisation rules";
+    return "";
+}
+
+std::string parse_gpf_text(const std::string &text, Gpf *g) {
+    // one integer per line with atoi semantics; values are kept as 32-bit words
+    std::vector<uint32_t> words;
+    size_t pos = 0;
+    while (pos < text.size()) {
+        size_t end = text.find('\n', pos);
+        if (end == std::string::npos) end = text.size();
+        std::string line = text.substr(pos, end - pos);
+        pos = end + 1;
+        size_t k = 0;
+        while (k < line.size() && (line[k] == ' ' || line[k] == '\t' || line[k] == '\r')) k++;
+        if (k == line.size()) continue;
+        words.push_back((uint32_t)std::strtoll(line.c_str() + k, nullptr, 10));
+    }
+    return parse_gpf_words(words.data(), words.size(), g);
+}
+
+std::string decode_gpf(const Gpf &g, Decoded *out) {
+    const uint32_t n = g.nr_procs;
+    if (g.bits_act < 1 || g.bits_act > 30) return "bits_act outside 1..30";
+    if (g.nbits_offset < 1 || g.nbits_offset > 31) return "nbits_offset outside 1..31";
+    if (g.nbits_syncbits_offset < 1 || g.nbits_syncbits_offset > 31) return "nbits_syncbits_offset outside 1..31";
+    if (g.firstbit[0] != 0) return "firstbit_statevector[0] != 0";
+    for (uint32_t p = 0; p < n; p++) {
+        if (g.bits_state[p] < 1 || g.bits_state[p] > 31 - g.bits_act) return "bits_state outside 1..31-bits_act";
+        if (g.firstbit[p + 1] != g.firstbit[p] + g.bits_state[p]) return "firstbit_statevector disagrees with bits_state";
+        if (g.proc_offsets_start[p + 1] < g.proc_offsets_start[p]) return "proc_offsets_start decreasing";
+    }
+    const uint32_t state_bits = g.firstbit[n];
+    const uint32_t per_off = 32 / g.nbits_offset;
+
+    // rules per action (GPUexplore.cu:998-1019): words [field a, field a+1) of syncbits
+    const uint32_t per_sync_off = 32 / g.nbits_syncbits_offset;
+    const uint64_t nact_fields = (uint64_t)g.nr_syncbits_offsets * per_sync_off;
+    auto rules_of = [&](uint32_t a, std::vector<uint32_t> *masks) -> std::string {
+        masks->clear();
+        if ((uint64_t)a + 1 >= nact_fields) return "";
+        uint32_t o1 = packed_field(g.syncbits_offsets.data(), a, g.nbits_syncbits_offset);
+        uint32_t o2 = packed_field(g.syncbits_offsets.data(), a + 1, g.nbits_syncbits_offset);
+        const uint32_t per_rule = 32 / n;
+        for (uint32_t w = o1; w < o2; w++) {
+            if (w >= g.nr_syncbits) return "synchronisation rule range past syncbits";
+            for (uint32_t f = 0; f < per_rule; f++) {
+                uint32_t r = (g.syncbits[w] >> (f * n)) & ((n == 32) ? 0xFFFFFFFFu : ((1u << n) - 1u));
+                if (r) masks->push_back(r);
+            }
+        }
+        return "";
+    };
+
+    // decode every (p, s) reachable in p's LTS from local state 0
+    struct PS {
+        std::vector<uint32_t> local;
+        std::map<uint32_t, std::vector<uint32_t>> sync;
+    };
+    std::vector<std::vector<PS>> ps(n);
+    std::vector<uint32_t> nstates(n);
+    for (uint32_t p = 0; p < n; p++) {
+        const uint32_t nwords = g.proc_offsets_start[p + 1] - g.proc_offsets_start[p];
+        const uint32_t nfields = nwords * per_off;
+        const uint32_t *base = g.proc_offsets.data() + g.proc_offsets_start[p];
+        const uint32_t w = g.bits_state[p], nslots = (31 - g.bits_act) / w;
+        std::vector<int> seen(1u << w, 0);
+        std::vector<uint32_t> todo{0};
+        seen[0] = 1;
+        uint32_t maxs = 0;
+        std::map<uint32_t, PS> dec;
+        while (!todo.empty()) {
+            uint32_t s = todo.back();
+            todo.pop_back();
+            maxs = std::max(maxs, s);
+            if (s + 1 >= nfields) return "transition offsets missing for a reachable local state";
+            uint32_t o1 = packed_field(base, s, g.nbits_offset);   // GPUexplore.cu:883-898
+            uint32_t o2 = packed_field(base, s + 1, g.nbits_offset);
+            PS &rec = dec[s];
+            for (uint32_t k = o1; k < o2; k++) {
+                if (k >= g.nr_trans) return "transition range past proc_trans";
+                uint32_t e = g.proc_trans[k];
+                std::vector<uint32_t> ts;
+                for (uint32_t i = 0; i < nslots; i++) {  // slots hold target+1 (GPUexplore.cu:159)
+                    uint32_t t = (e >> (1 + g.bits_act + i * w)) & ((1u << w) - 1u);
+                    if (!t) break;
+                    ts.push_back(t - 1);
+                }
+                if (ts.empty()) return "transition entry without targets";
+                std::vector<uint32_t> &dst =
+                    (e & 1u) ? rec.sync[(e >> 1) & ((1u << g.bits_act) - 1u)] : rec.local;
+                for (uint32_t t : ts) {
+                    if (std::find(dst.begin(), dst.end(), t) == dst.end()) dst.push_back(t);
+                    if (!seen[t]) {
+                        seen[t] = 1;
+                        todo.push_back(t);
+                    }
+                }
+            }
+        }
+        nstates[p] = maxs + 1;
+        ps[p].resize(nstates[p]);
+        for (auto &kv : dec) ps[p][kv.first] = kv.second;
+    }
+    if (state_bits > (uint32_t)kMaxStateBits) return "UNSUPPORTED: state vector wider than 126 bits";
+
+    // rules, and per (p, s) the rules p leads (lowest member) for actions p has enabled
+    std::vector<uint32_t> rule_mask, rule_act;
+    std::map<uint32_t, std::pair<uint32_t, uint32_t>> rules_range; // action -> [first, count)
+    std::set<uint32_t> actions;
+    for (uint32_t p = 0; p < n; p++)
+        for (auto &r : ps[p])
+            for (auto &kv : r.sync) actions.insert(kv.first);
+    std::vector<uint32_t> masks;
+    for (uint32_t a : actions) {
+        std::string err = rules_of(a, &masks);
+        if (!err.empty()) return err;
+        rules_range[a] = {(uint32_t)rule_mask.size(), (uint32_t)masks.size()};
+        for (uint32_t m : masks) {
+            rule_mask.push_back(m);
+            rule_act.push_back(a);
+        }
+    }
+
+    std::vector<uint32_t> recs, ltgt, sent, stgt, lrule;
+    std::vector<uint32_t> psbase(n + 1, 0);
+    uint32_t max_lrules = 0;
+    for (uint32_t p = 0; p < n; p++) {
+        psbase[p] = (uint32_t)(recs.size() / kRecWords);
+        for (uint32_t s = 0; s < nstates[p]; s++) {
+            const PS &r = ps[p][s];
+            uint32_t rec[kRecWords] = {0};
+            rec[R_LOFF] = (uint32_t)ltgt.size();
+            rec[R_LCNT] = (uint32_t)r.local.size();
+            for (uint32_t t : r.local) {
+                ltgt.push_back(t);
+                if (t == 1) rec[R_FLAGS] |= 1u;
+            }
+            rec[R_SOFF] = (uint32_t)(sent.size() / 4);
+            rec[R_SCNT] = (uint32_t)r.sync.size();
+            rec[R_ROFF] = (uint32_t)lrule.size();
+            uint32_t cl0 = 1u << p;
+            for (auto &kv : r.sync) {  // ascending action order
+                uint32_t has1 = 0;
+                uint32_t toff = (uint32_t)stgt.size();
+                for (uint32_t t : kv.second) {
+                    stgt.push_back(t);
+                    if (t == 1) has1 = 1;
+                }
+                sent.push_back(kv.first);
+                sent.push_back(toff);
+                sent.push_back((uint32_t)kv.second.size());
+                sent.push_back(has1);
+                auto rr = rules_range[kv.first];
+                for (uint32_t k = rr.first; k < rr.first + rr.second; k++) {
+                    uint32_t m = rule_mask[k];
+                    if (m >> p & 1u) cl0 |= m; // GPUexplore.cu:1616-1624
+                    if ((uint32_t)__builtin_ctz(m) == p) lrule.push_back(k);
+                }
+            }
+            rec[R_RCNT] = (uint32_t)lrule.size() - rec[R_ROFF];
+            rec[R_CL0] = cl0;
+            max_lrules = std::max(max_lrules, rec[R_RCNT]);
+            recs.insert(recs.end(), rec, rec + kRecWords);
+        }
+    }
+    psbase[n] = (uint32_t)(recs.size() / kRecWords);
+    if (max_lrules > 32) return "UNSUPPORTED: a process leads more than 32 rules in one local state";
+
+    std::vector<uint32_t> &wds = out->words;
+    wds.assign(kHdrWords, 0);
+    wds[H_NPROCS] = n;
+    wds[H_STATE_BITS] = state_bits;
+    for (uint32_t p = 0; p <= n; p++) wds[H_FB + p] = g.firstbit[p];
+    for (uint32_t p = 0; p < n; p++) wds[H_BS + p] = g.bits_state[p];
+    for (uint32_t p = 0; p <= n; p++) wds[H_PSBASE + p] = psbase[p];
+    auto append = [&](const std::vector<uint32_t> &v) {
+        uint32_t off = (uint32_t)wds.size();
+        wds.insert(wds.end(), v.begin(), v.end());
+        while (wds.size() % 4) wds.push_back(0); // keep every array 16-byte aligned
+        return off;
+    };
+    wds[H_OFF_RECS] = append(recs);
+    wds[H_OFF_LTGT] = append(ltgt);
+    wds[H_OFF_SENT] = append(sent);
+    wds[H_OFF_STGT] = append(stgt);
+    std::vector<uint32_t> rules;
+    for (size_t k = 0; k < rule_mask.size(); k++) {
+        rules.push_back(rule_mask[k]);
+        rules.push_back(rule_act[k]);
+    }
+    wds[H_OFF_RULES] = append(rules);
+    wds[H_OFF_LRULE] = append(lrule);
+    wds[H_NRULES] = (uint32_t)rule_mask.size();
+    wds[H_TOTAL_WORDS] = (uint32_t)wds.size();
+    wds[H_MAX_LRULES] = max_lrules;
+    out->nprocs = n;
+    out->state_bits = state_bits;
+    out->key_words = state_bits ? (state_bits + 31) / 32 : 1;
+    out->nstates = nstates;
+    return "";
+}
+
+} // namespace gpx

@@ -1,0 +1,266 @@
+"""Seeded generators of gpf networks (the reference's model generator and model
+set are not available, so the benchmark and test networks are built here).
+
+Every generator is a pure function of its seed (Python's `random.Random`, so the
+same file is produced on any host).  The generated networks keep to the subset
+of the gpf semantics on which the reference's two successor kernels agree
+(GPUexplore.cu:756-1189 vs 1191-1733): every synchronisation rule has at least
+two participants, one (process, state, action) never needs more than two
+transition entries (max_buf_ints <= 2), and targets are never repeated.
+
+Families
+--------
+ring            ring of n processes, each an m-state LTS with one local tau edge
+                and two handshake actions with its neighbours (rule {i, i+1})
+random_network  n processes with U[lo, hi] states, out-degree U[1, 4], a share of
+                the transitions synchronising 2-3 processes, and optionally an
+                embedded safety monitor over a seeded pair of error local states
+clustered       processes in seeded clusters, transitions mostly inside the
+                cluster (tau or intra-cluster sync) and a share of
+                cross-cluster synchronisations
+batch           many random networks of uneven sizes
+"""
+from __future__ import annotations
+
+import random
+from typing import Dict, List, Optional, Tuple
+
+from .gpf import Network
+
+
+def _empty(nstates: List[int]) -> Network:
+    return Network(
+        nstates=list(nstates),
+        local=[[[] for _ in range(ns)] for ns in nstates],
+        sync=[[{} for _ in range(ns)] for ns in nstates],
+        rules={},
+    )
+
+
+def _add_sync(net: Network, p: int, s: int, a: int, t: int) -> bool:
+    ts = net.sync[p][s].setdefault(a, [])
+    if t in ts:
+        return False
+    ts.append(t)
+    return True
+
+
+def _add_local(net: Network, p: int, s: int, t: int) -> bool:
+    if t in net.local[p][s]:
+        return False
+    net.local[p][s].append(t)
+    return True
+
+
+def ring(seed: int, nprocs: int = 8, nstates: int = 5, p_sync: float = 0.9) -> Network:
+    """Ring of `nprocs` processes with `nstates` local states each.
+
+    Process i has one local tau edge (a seeded state to a seeded other state) and
+    takes part in two handshake actions: h_i with its right neighbour (rule
+    {i, i+1 mod n}) and h_{i-1} with its left neighbour.  Each state offers each
+    handshake with probability `p_sync`, to a seeded target.  The seed also picks
+    each process's initial local state; states are relabelled so that it is 0
+    (the reference's initial state is the all-zero vector, GPUexplore.cu:673-676).
+    """
+    rng = random.Random(seed)
+    net = _empty([nstates] * nprocs)
+    for a in range(nprocs):
+        net.rules[a] = [(1 << a) | (1 << ((a + 1) % nprocs))]
+    for i in range(nprocs):
+        init = rng.randrange(nstates)
+        perm = list(range(nstates))
+        perm[0], perm[init] = perm[init], perm[0]  # relabel: seeded initial state -> 0
+        src = rng.randrange(nstates)
+        tgt = rng.choice([x for x in range(nstates) if x != src])
+        _add_local(net, i, perm[src], perm[tgt])
+        for s in range(nstates):
+            for a in (i, (i - 1) % nprocs):
+                if rng.random() < p_sync:
+                    _add_sync(net, i, perm[s], a, perm[rng.randrange(nstates)])
+    return net
+
+
+def add_safety_monitor(net: Network, i: int, a: int, j: int, b: int) -> Network:
+    """Embed the safety property "never process i in local state a while process j
+    is in local state b" as a monitor process appended last.
+
+    The reference checks a safety property as "the last process reaches local
+    state 1" (GPUexplore.cu:927-935, 1063-1069).  Every local transition of i that
+    enters or leaves a (and of j for b) becomes a two-party synchronisation with the
+    monitor, whose four states track (i in a, j in b): 0 = neither, 1 = both (the
+    error state), 2 = only i in a, 3 = only j in b.  The monitor enables every
+    action it observes in every state where it can occur, so it never blocks and
+    the reachable state count equals that of the unmonitored network.
+    Requires a != 0, b != 0 (the initial state maps to monitor state 0) and that
+    no synchronising transition of i (j) enters or leaves a (b).
+    """
+    if i == j or a == 0 or b == 0:
+        raise ValueError("need two distinct processes and nonzero error states")
+    n = net.nprocs
+    M = n
+    base = net.nactions()
+    E_i, L_i, E_j, L_j = base, base + 1, base + 2, base + 3
+    out = Network(
+        nstates=net.nstates + [4],
+        local=[[list(ts) for ts in net.local[p]] for p in range(n)] + [[[] for _ in range(4)]],
+        sync=[[dict((k, list(v)) for k, v in d.items()) for d in net.sync[p]] for p in range(n)]
+        + [[{} for _ in range(4)]],
+        rules=dict((k, list(v)) for k, v in net.rules.items()),
+        liveness=net.liveness,
+    )
+    for proc, err, enter, leave in ((i, a, E_i, L_i), (j, b, E_j, L_j)):
+        for s in range(out.nstates[proc]):
+            for aa, ts in out.sync[proc][s].items():
+                for t in ts:
+                    if (s == err) != (t == err):
+                        raise ValueError("a synchronising transition crosses an error state")
+            keep = []
+            for t in out.local[proc][s]:
+                if s != err and t == err:
+                    _add_sync(out, proc, s, enter, t)
+                elif s == err and t != err:
+                    _add_sync(out, proc, s, leave, t)
+                else:
+                    keep.append(t)
+            out.local[proc][s] = keep
+        out.rules[enter] = [(1 << proc) | (1 << M)]
+        out.rules[leave] = [(1 << proc) | (1 << M)]
+    # monitor transitions: states 0=(-A,-B) 1=(A,B) 2=(A,-B) 3=(-A,B)
+    for act, moves in ((E_i, ((0, 2), (3, 1))), (L_i, ((2, 0), (1, 3))),
+                       (E_j, ((0, 3), (2, 1))), (L_j, ((3, 0), (1, 2)))):
+        for s, t in moves:
+            _add_sync(out, M, s, act, t)
+    return out
+
+
+def _sync_pool(rng: random.Random, procs: List[int], nactions: int,
+               parties: Tuple[int, int], groups: Optional[List[List[int]]] = None,
+               p_subrule: float = 0.25) -> Tuple[Dict[int, List[int]], List[List[int]]]:
+    """Create `nactions` synchronising actions over `procs`; return (rules, per-process action lists)."""
+    rules: Dict[int, List[int]] = {}
+    acts_of: Dict[int, List[int]] = {p: [] for p in procs}
+    for a in range(nactions):
+        pool = procs if groups is None else rng.choice(groups)
+        k = min(len(pool), rng.randint(parties[0], parties[1]))
+        if k < 2:
+            continue
+        members = sorted(rng.sample(pool, k))
+        mask = 0
+        for p in members:
+            mask |= 1 << p
+        rs = [mask]
+        if k >= 3 and rng.random() < p_subrule:
+            sub = sorted(rng.sample(members, 2))
+            rs.append((1 << sub[0]) | (1 << sub[1]))
+        rules[a] = rs
+        for p in members:
+            acts_of[p].append(a)
+    return rules, [acts_of[p] for p in sorted(acts_of)]
+
+
+def random_network(seed: int, nprocs: int = 16, states: Tuple[int, int] = (8, 32),
+                   outdeg: Tuple[int, int] = (1, 4), sync_frac: float = 0.2,
+                   parties: Tuple[int, int] = (2, 3), safety: bool = True,
+                   nactions: Optional[int] = None) -> Network:
+    """Random network: `nprocs` processes with U[states] local states, out-degree
+    U[outdeg] per state, each transition synchronising with probability
+    `sync_frac` (an action shared by 2-3 seeded processes), otherwise local.
+    With `safety`, a monitor over a seeded pair of error local states is
+    appended (see :func:`add_safety_monitor`), giving nprocs+1 processes."""
+    rng = random.Random(seed)
+    nst = [rng.randint(states[0], states[1]) for _ in range(nprocs)]
+    net = _empty(nst)
+    na = nactions if nactions is not None else 2 * nprocs
+    rules, acts_of = _sync_pool(rng, list(range(nprocs)), na, parties)
+    net.rules = rules
+    err = None
+    if safety:
+        i, j = rng.sample(range(nprocs), 2)
+        err = {i: rng.randrange(1, nst[i]), j: rng.randrange(1, nst[j])}
+    for p in range(nprocs):
+        for s in range(nst[p]):
+            for _ in range(rng.randint(outdeg[0], outdeg[1])):
+                t = rng.randrange(nst[p])
+                crosses = err is not None and p in err and ((s == err[p]) != (t == err[p]))
+                if acts_of[p] and rng.random() < sync_frac and not crosses:
+                    _add_sync(net, p, s, rng.choice(acts_of[p]), t)
+                else:
+                    _add_local(net, p, s, t)
+    _prune_unused_rules(net)
+    if safety:
+        (i, a), (j, b) = sorted(err.items())
+        net = add_safety_monitor(net, i, a, j, b)
+    return net
+
+
+def clustered(seed: int, nprocs: int = 24, nclusters: Tuple[int, int] = (4, 6),
+              states: Tuple[int, int] = (3, 6), outdeg: Tuple[int, int] = (1, 3),
+              p_tau: float = 0.5, p_intra: float = 0.3) -> Network:
+    """Processes in U[nclusters] seeded clusters: a transition is a local tau with
+    probability p_tau, an intra-cluster synchronisation with probability p_intra and
+    a cross-cluster synchronisation otherwise (the default mix is 80% inside the
+    cluster, 20% across)."""
+    rng = random.Random(seed)
+    k = rng.randint(nclusters[0], nclusters[1])
+    procs = list(range(nprocs))
+    rng.shuffle(procs)
+    groups = [sorted(procs[c::k]) for c in range(k)]
+    cluster_of = {p: c for c, g in enumerate(groups) for p in g}
+    nst = [rng.randint(states[0], states[1]) for _ in range(nprocs)]
+    net = _empty(nst)
+    intra_rules, intra_acts = _sync_pool(rng, list(range(nprocs)), 2 * nprocs, (2, 2),
+                                         groups=[g for g in groups if len(g) >= 2], p_subrule=0.0)
+    cross_rules: Dict[int, List[int]] = {}
+    cross_acts: Dict[int, List[int]] = {p: [] for p in range(nprocs)}
+    base = 2 * nprocs
+    for a in range(nprocs):
+        c1, c2 = rng.sample(range(k), 2)
+        p1, p2 = rng.choice(groups[c1]), rng.choice(groups[c2])
+        cross_rules[base + a] = [(1 << p1) | (1 << p2)]
+        cross_acts[p1].append(base + a)
+        cross_acts[p2].append(base + a)
+    net.rules = dict(intra_rules)
+    net.rules.update(cross_rules)
+    for p in range(nprocs):
+        for s in range(nst[p]):
+            for _ in range(rng.randint(outdeg[0], outdeg[1])):
+                t = rng.randrange(nst[p])
+                x = rng.random()
+                if x < p_tau or (x < p_tau + p_intra and not intra_acts[p]) or \
+                        (x >= p_tau + p_intra and not cross_acts[p]):
+                    _add_local(net, p, s, t)
+                elif x < p_tau + p_intra:
+                    _add_sync(net, p, s, rng.choice(intra_acts[p]), t)
+                else:
+                    _add_sync(net, p, s, rng.choice(cross_acts[p]), t)
+    del cluster_of
+    _prune_unused_rules(net)
+    return net
+
+
+def batch(seed: int, count: int = 512, procs: Tuple[int, int] = (4, 24),
+          states: Tuple[int, int] = (4, 32)) -> List[Network]:
+    """`count` random networks of uneven sizes (process counts and local state
+    counts drawn per network)."""
+    rng = random.Random(seed)
+    nets = []
+    for _ in range(count):
+        n = rng.randint(procs[0], procs[1])
+        hi = rng.randint(states[0], states[1])
+        nets.append(random_network(rng.randrange(1 << 30), nprocs=n, states=(states[0], hi),
+                                   outdeg=(1, 3), safety=rng.random() < 0.5))
+    return nets
+
+
+def _prune_unused_rules(net: Network) -> None:
+    used = set()
+    for p in range(net.nprocs):
+        for d in net.sync[p]:
+            used.update(d)
+    net.rules = {a: rs for a, rs in net.rules.items() if a in used}
+    # compact action ids so bits_act stays small
+    order = sorted(used | set(net.rules))
+    remap = {a: i for i, a in enumerate(order)}
+    net.rules = {remap[a]: rs for a, rs in net.rules.items()}
+    for p in range(net.nprocs):
+        net.sync[p] = [{remap[a]: ts for a, ts in d.items()} for d in net.sync[p]]

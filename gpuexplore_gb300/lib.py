@@ -1,0 +1,288 @@
+"""ctypes binding of libgpx (include/gpx.h).
+
+The library is the product: every exploration here runs the CUDA kernels in
+``_lib/libgpx.so``.  Loading fails loudly when the library has not been built;
+there is no fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from .build import LIB
+
+GPX_OK = 0
+STATUS = ["ok", "parse", "no_gpu", "cuda", "table_full", "timeout", "invalid", "unsupported", "store_full", "nomem"]
+PROP_NONE, PROP_DEADLOCK, PROP_SAFETY, PROP_LIVENESS = 0, 1, 2, 3
+PROPERTIES = {"none": PROP_NONE, "deadlock": PROP_DEADLOCK, "safety": PROP_SAFETY, "liveness": PROP_LIVENESS}
+VERDICTS = {v: k for k, v in PROPERTIES.items()}
+STOPS = ["done", "violation", "budget", "error"]
+
+EXPORTS = [
+    "gpx_status_string", "gpx_abi_version", "gpx_device_info_get", "gpx_options_init", "gpx_model_load",
+    "gpx_model_load_file", "gpx_model_from_words", "gpx_model_info_get", "gpx_model_free", "gpx_explore",
+    "gpx_explorer_create", "gpx_explorer_run", "gpx_explorer_set_model", "gpx_explorer_destroy",
+    "gpx_result_free", "gpx_explorer_dump",
+]
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32), ("blocks", C.c_int32), ("threads", C.c_int32),
+        ("kernel_iters", C.c_int32), ("verbosity", C.c_int32), ("q_words", C.c_uint64),
+        ("por", C.c_int32), ("cycle_proviso", C.c_int32), ("property", C.c_int32), ("device", C.c_int32),
+        ("seed", C.c_uint64), ("max_states", C.c_uint64), ("store_states", C.c_uint64),
+        ("collect_states", C.c_int32), ("bucket_bytes", C.c_int32),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32), ("status", C.c_int32), ("stopped", C.c_int32), ("verdict", C.c_int32),
+        ("states", C.c_uint64), ("nlevels", C.c_uint32), ("level_counts", C.POINTER(C.c_uint64)),
+        ("transitions", C.c_uint64), ("probes", C.c_uint64), ("launches", C.c_uint64),
+        ("explore_ms", C.c_double), ("setup_ms", C.c_double), ("set_hash", C.c_uint64),
+        ("key_words", C.c_uint32), ("table_count", C.c_uint64), ("lookups", C.c_uint64),
+        ("expanded", C.c_uint64), ("kernel_ms", C.c_double), ("states_buf", C.POINTER(C.c_uint32)),
+        ("table_slots", C.c_uint64), ("slot_bytes", C.c_uint32), ("blocks", C.c_uint32), ("threads", C.c_uint32),
+    ]
+
+
+class ModelInfo(C.Structure):
+    _fields_ = [
+        ("liveness", C.c_uint32), ("nr_procs", C.c_uint32), ("bits_act", C.c_uint32),
+        ("proc_nrstates", C.c_uint32), ("bits_statevector", C.c_uint32), ("nbits_offset", C.c_uint32),
+        ("max_buf_ints", C.c_uint32), ("nr_trans", C.c_uint32), ("state_bits", C.c_uint32),
+        ("key_words", C.c_uint32), ("firstbit", C.c_uint32 * 33), ("bits_state", C.c_uint32 * 32),
+    ]
+
+
+class DeviceInfo(C.Structure):
+    _fields_ = [
+        ("total_global_mem", C.c_uint64), ("shared_mem_per_block", C.c_int32), ("shared_mem_per_sm", C.c_int32),
+        ("max_threads_per_block", C.c_int32), ("max_grid_size", C.c_int32), ("sm_count", C.c_int32),
+        ("name", C.c_char * 256),
+    ]
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def load(path: str = LIB) -> C.CDLL:
+    """Load libgpx.so (build it first with gpuexplore_gb300.build.build_all)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libgpx is not built ({path} missing): run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    vp, i, u32p = C.c_void_p, C.c_int, C.POINTER(C.c_uint32)
+    lib.gpx_status_string.restype = C.c_char_p
+    lib.gpx_status_string.argtypes = [i]
+    lib.gpx_abi_version.restype = i
+    lib.gpx_device_info_get.argtypes = [i, C.POINTER(DeviceInfo)]
+    lib.gpx_options_init.argtypes = [C.POINTER(Options)]
+    lib.gpx_options_init.restype = None
+    lib.gpx_model_load.argtypes = [C.c_char_p, C.POINTER(vp)]
+    lib.gpx_model_load_file.argtypes = [C.c_char_p, C.POINTER(vp)]
+    lib.gpx_model_from_words.argtypes = [u32p, C.c_size_t, C.POINTER(vp)]
+    lib.gpx_model_info_get.argtypes = [vp, C.POINTER(ModelInfo)]
+    lib.gpx_model_free.argtypes = [vp]
+    lib.gpx_model_free.restype = None
+    lib.gpx_explore.argtypes = [vp, C.POINTER(Options), C.POINTER(Result)]
+    lib.gpx_explorer_create.argtypes = [vp, C.POINTER(Options), C.POINTER(vp)]
+    lib.gpx_explorer_run.argtypes = [vp, C.POINTER(Result)]
+    lib.gpx_explorer_set_model.argtypes = [vp, vp]
+    lib.gpx_explorer_destroy.argtypes = [vp]
+    lib.gpx_explorer_destroy.restype = None
+    lib.gpx_result_free.argtypes = [C.POINTER(Result)]
+    lib.gpx_result_free.restype = None
+    lib.gpx_explorer_dump.argtypes = [vp, C.c_char_p]
+    _lib = lib
+    return lib
+
+
+class GpxError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        name = STATUS[status] if 0 <= status < len(STATUS) else str(status)
+        super().__init__(f"{what}: gpx status {status} ({name})")
+
+
+def options(**kw) -> Options:
+    """Options with the library defaults, then the given fields (property may be a name)."""
+    lib = load()
+    o = Options()
+    lib.gpx_options_init(C.byref(o))
+    for k, v in kw.items():
+        if k == "property" and isinstance(v, str):
+            v = PROPERTIES[v]
+        setattr(o, k, int(v))
+    return o
+
+
+class Model:
+    """A loaded gpf network (owned handle)."""
+
+    def __init__(self, handle: int):
+        self.handle = C.c_void_p(handle)
+
+    @classmethod
+    def from_file(cls, path: str) -> "Model":
+        lib = load()
+        h = C.c_void_p()
+        rc = lib.gpx_model_load_file(path.encode(), C.byref(h))
+        if rc != GPX_OK:
+            raise GpxError(rc, f"loading {path}")
+        return cls(h.value)
+
+    @classmethod
+    def from_words(cls, words: Sequence[int]) -> "Model":
+        lib = load()
+        arr = np.ascontiguousarray(np.asarray(words, dtype=np.uint64).astype(np.uint32))
+        h = C.c_void_p()
+        rc = lib.gpx_model_from_words(arr.ctypes.data_as(C.POINTER(C.c_uint32)), arr.size, C.byref(h))
+        if rc != GPX_OK:
+            raise GpxError(rc, "parsing gpf words")
+        return cls(h.value)
+
+    def info(self) -> ModelInfo:
+        inf = ModelInfo()
+        rc = load().gpx_model_info_get(self.handle, C.byref(inf))
+        if rc != GPX_OK:
+            raise GpxError(rc, "model info")
+        return inf
+
+    def close(self) -> None:
+        if self.handle:
+            load().gpx_model_free(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _result_dict(r: Result) -> Dict:
+    levels = [int(r.level_counts[i]) for i in range(r.nlevels)] if r.level_counts else []
+    d = {
+        "status": int(r.status), "stopped": STOPS[r.stopped] if 0 <= r.stopped < 4 else str(r.stopped),
+        "verdict": VERDICTS.get(int(r.verdict), str(r.verdict)), "states": int(r.states), "levels": levels,
+        "transitions": int(r.transitions), "probes": int(r.probes), "lookups": int(r.lookups),
+        "expanded": int(r.expanded), "launches": int(r.launches), "explore_ms": float(r.explore_ms),
+        "kernel_ms": float(r.kernel_ms), "setup_ms": float(r.setup_ms), "set_hash": f"{r.set_hash:016x}",
+        "key_words": int(r.key_words), "table_count": int(r.table_count), "table_slots": int(r.table_slots),
+        "slot_bytes": int(r.slot_bytes), "blocks": int(r.blocks), "threads": int(r.threads),
+    }
+    if r.states_buf:
+        n = r.states * r.key_words
+        buf = np.ctypeslib.as_array(r.states_buf, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+        d["states_words"] = buf.reshape(-1, r.key_words) if r.key_words else buf
+    return d
+
+
+class Explorer:
+    """A reusable explorer: device memory is allocated once; each run() resets it."""
+
+    def __init__(self, model: Model, opts: Options):
+        lib = load()
+        self.model = model
+        h = C.c_void_p()
+        rc = lib.gpx_explorer_create(model.handle, C.byref(opts), C.byref(h))
+        if rc != GPX_OK:
+            raise GpxError(rc, "creating explorer")
+        self.handle = h
+
+    def run(self, check: bool = True) -> Dict:
+        lib = load()
+        r = Result()
+        rc = lib.gpx_explorer_run(self.handle, C.byref(r))
+        try:
+            d = _result_dict(r)
+        finally:
+            lib.gpx_result_free(C.byref(r))
+        if check and rc != GPX_OK:
+            raise GpxError(rc, "exploring")
+        d["rc"] = rc
+        return d
+
+    def set_model(self, model: Model) -> None:
+        rc = load().gpx_explorer_set_model(self.handle, model.handle)
+        if rc != GPX_OK:
+            raise GpxError(rc, "replacing model")
+        self.model = model
+
+    def dump(self, path: str) -> None:
+        rc = load().gpx_explorer_dump(self.handle, path.encode())
+        if rc != GPX_OK:
+            raise GpxError(rc, "dumping")
+
+    def close(self) -> None:
+        if self.handle:
+            load().gpx_explorer_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def explore(path_or_model, check: bool = True, **kw) -> Dict:
+    """One-shot exploration of a gpf file (or Model) through gpx_explore."""
+    lib = load()
+    model = path_or_model if isinstance(path_or_model, Model) else Model.from_file(path_or_model)
+    o = options(**kw)
+    r = Result()
+    rc = lib.gpx_explore(model.handle, C.byref(o), C.byref(r))
+    try:
+        d = _result_dict(r)
+    finally:
+        lib.gpx_result_free(C.byref(r))
+    if check and rc != GPX_OK:
+        raise GpxError(rc, "exploring")
+    d["rc"] = rc
+    return d
+
+
+def device_info(device: int = 0) -> Optional[DeviceInfo]:
+    inf = DeviceInfo()
+    rc = load().gpx_device_info_get(device, C.byref(inf))
+    return inf if rc == GPX_OK else None
+
+
+def states_set_hash(words: np.ndarray) -> str:
+    """Order-independent set hash of state-vector rows (same formula as the oracle and libgpx)."""
+    words = np.asarray(words, dtype=np.uint64)
+    if words.ndim == 1:
+        words = words[:, None]
+    M = np.uint64(0xFFFFFFFFFFFFFFFF)
+    with np.errstate(over="ignore"):
+        h = np.full(words.shape[0], 0x9E3779B97F4A7C15, dtype=np.uint64)
+        for j in range(0, words.shape[1], 2):
+            c = words[:, j].copy()
+            if j + 1 < words.shape[1]:
+                c |= words[:, j + 1] << np.uint64(32)
+            z = (h ^ c) + np.uint64(0x9E3779B97F4A7C15)
+            z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+            z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+            h = z ^ (z >> np.uint64(31))
+        total = int(h.sum(dtype=np.uint64)) & int(M)
+    return f"{total:016x}"
+
+
+def exported_symbols(path: str = LIB) -> List[str]:
+    lib = C.CDLL(path)
+    return [s for s in EXPORTS if hasattr(lib, s)]

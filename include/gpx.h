@@ -1,0 +1,163 @@
+/*
+ * gpx.h -- C ABI of libgpx, the GB300 (sm_103a) state-space explorer.
+ *
+ * The reference (GPUexplore) has no library API: its boundary is the process
+ * level -- `GPUexplore <model> [options]`, a <model>.gpf file and stdout lines
+ * (GPUexplore/src/GPUexplore.cu:1738-2188).  This header exposes that boundary
+ * as plain C entry points (plain pointers and sizes, no C++ or torch types) so a
+ * C, C++, Python (ctypes) or other FFI caller can drive the same exploration
+ * in-process; the `gpuexplore` command-line tool is a thin client of it.
+ *
+ * Threading: a gpx_explorer is used by one host thread at a time.  Calls block
+ * until the device work they start has finished.  One device per explorer.
+ */
+#ifndef GPX_H
+#define GPX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPX_ABI_VERSION 1
+
+/* Status codes.  They replace the reference's exit(1) paths. */
+typedef enum {
+    GPX_OK = 0,
+    GPX_ERR_PARSE = 1,       /* missing or malformed gpf input (GPUexplore.cu:1984-1987) */
+    GPX_ERR_NO_GPU = 2,      /* no CUDA device (GPUexplore.cu:1999-2003) */
+    GPX_ERR_CUDA = 3,        /* a CUDA runtime call failed (CUDA_CHECK_RETURN, GPUexplore.cu:522-528) */
+    GPX_ERR_TABLE_FULL = 4,  /* every probe bucket of a state was full ("problem with hash table",
+                                contBFS == 2, GPUexplore.cu:1170-1173, 2164-2166) */
+    GPX_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up (no reference counterpart) */
+    GPX_ERR_INVALID = 6,     /* invalid argument */
+    GPX_ERR_UNSUPPORTED = 7, /* model outside this build's limits (state vector > 126 bits,
+                                > 31 processes) */
+    GPX_ERR_STORE_FULL = 8,  /* the state store (the BFS queue of visited states) overflowed */
+    GPX_ERR_NOMEM = 9        /* device or host allocation failed */
+} gpx_status;
+
+/* Property to check (PropertyStatus, GPUexplore.cu:27). */
+typedef enum {
+    GPX_PROP_NONE = 0,
+    GPX_PROP_DEADLOCK = 1, /* -d */
+    GPX_PROP_SAFETY = 2,   /* -p: last process reaches local state 1 */
+    GPX_PROP_LIVENESS = 3  /* -p with gpf line 1 == 1; parsed, never checked (as in the reference) */
+} gpx_property;
+
+typedef enum {
+    GPX_STOP_DONE = 0,      /* no unexplored states left */
+    GPX_STOP_VIOLATION = 1, /* property violated; stopped at the end of that BFS level */
+    GPX_STOP_BUDGET = 2,    /* max_states reached at the end of a level */
+    GPX_STOP_ERROR = 3      /* see gpx_result.status */
+} gpx_stop;
+
+/* Options: the reference's command-line flags (GPUexplore.cu:1785-1883) plus
+ * the controls this build adds.  Initialise with gpx_options_init(). */
+typedef struct {
+    uint32_t struct_size;   /* sizeof(gpx_options), set by gpx_options_init */
+    int32_t blocks;         /* -b: blocks of the persistent kernel (0 = every SM, full occupancy) */
+    int32_t threads;        /* -t: threads per block (0 = 256) */
+    int32_t kernel_iters;   /* -k: BFS levels per kernel launch (0 = run to the end in one launch) */
+    int32_t verbosity;      /* -v 0..3 (clamped to 3, GPUexplore.cu:1846-1848) */
+    uint64_t q_words;       /* -q: hash-table size in 32-bit words (0 = half the free device memory) */
+    int32_t por;            /* --por: cluster-based ample-set reduction */
+    int32_t cycle_proviso;  /* --cycle-proviso */
+    int32_t property;       /* gpx_property */
+    int32_t device;         /* CUDA device ordinal */
+    uint64_t seed;          /* seed of the hash functions (does not affect any result) */
+    uint64_t max_states;    /* stop at the end of the level that reaches this many states (0 = off) */
+    uint64_t store_states;  /* capacity of the state store in states (0 = as many as table slots) */
+    int32_t collect_states; /* copy the visited states back into gpx_result.states */
+    int32_t bucket_bytes;   /* hash bucket size: 32 (one DRAM sector) or 64; 0 = automatic */
+} gpx_options;
+
+/* Result of one exploration.  Arrays are owned by the library: gpx_result_free. */
+typedef struct {
+    uint32_t struct_size;
+    int32_t status;          /* gpx_status of the run */
+    int32_t stopped;         /* gpx_stop */
+    int32_t verdict;         /* gpx_property that was violated, or GPX_PROP_NONE */
+    uint64_t states;         /* visited states ("nr. of states in hash table", GPUexplore.cu:2172) */
+    uint32_t nlevels;        /* BFS levels discovered, level 0 = the initial state */
+    uint64_t *level_counts;  /* new states per level [nlevels] */
+    uint64_t transitions;    /* successor instances generated */
+    uint64_t probes;         /* hash-bucket probes (lookups and inserts) */
+    uint64_t launches;       /* kernel launches of the exploration loop */
+    double explore_ms;       /* device time of the exploration (CUDA events) */
+    double setup_ms;         /* host time spent on table reset and model upload */
+    uint64_t set_hash;       /* order-independent hash of the visited set (sum of key hashes) */
+    uint32_t key_words;      /* 32-bit words per state vector in `states_buf` */
+    uint64_t table_count;    /* occupied hash-table slots, counted by a sweep like count_states
+                                (GPUexplore.cu:687-704); filled when collect_states or verbosity >= 2 */
+    uint64_t lookups;        /* successors looked up in the hash table */
+    uint64_t expanded;       /* frontier states expanded */
+    double kernel_ms;        /* device time of the exploration kernel launches only */
+    uint32_t *states_buf;    /* visited states [states * key_words] in BFS order, when collected */
+    uint64_t table_slots;    /* hash-table capacity in states */
+    uint32_t slot_bytes;     /* bytes per hash-table slot (4, 8 or 16) */
+    uint32_t blocks, threads;/* launch configuration that ran */
+} gpx_result;
+
+typedef struct gpx_model gpx_model;
+typedef struct gpx_explorer gpx_explorer;
+
+/* Scalar facts of a loaded model (the header lines GPUexplore.cu:1890-1953 print). */
+typedef struct {
+    uint32_t liveness, nr_procs, bits_act, proc_nrstates, bits_statevector;
+    uint32_t nbits_offset, max_buf_ints, nr_trans;
+    uint32_t state_bits;     /* firstbit_statevector[nr_procs] */
+    uint32_t key_words;      /* ceil(state_bits / 32) */
+    uint32_t firstbit[33];
+    uint32_t bits_state[32];
+} gpx_model_info;
+
+/* Device facts the reference prints at start-up (GPUexplore.cu:2004-2010). */
+typedef struct {
+    uint64_t total_global_mem;
+    int32_t shared_mem_per_block, shared_mem_per_sm, max_threads_per_block, max_grid_size, sm_count;
+    char name[256];
+} gpx_device_info;
+
+const char *gpx_status_string(int status);
+int gpx_abi_version(void);
+/* GPX_ERR_NO_GPU when no CUDA device is present (GPUexplore.cu:1999-2003). */
+int gpx_device_info_get(int device, gpx_device_info *info);
+
+void gpx_options_init(gpx_options *opts);
+
+/* Load <path_without_ext>.gpf, appending the extension like GPUexplore.cu:1814-1815. */
+int gpx_model_load(const char *path_without_ext, gpx_model **out);
+/* Load a gpf file by its exact path. */
+int gpx_model_load_file(const char *path, gpx_model **out);
+/* Parse gpf integers already in host memory (one integer per gpf line). */
+int gpx_model_from_words(const uint32_t *words, size_t nwords, gpx_model **out);
+int gpx_model_info_get(const gpx_model *model, gpx_model_info *info);
+void gpx_model_free(gpx_model *model);
+
+/* One-shot exploration: allocate, explore, free (the reference's main, GPUexplore.cu:1989-2172). */
+int gpx_explore(const gpx_model *model, const gpx_options *opts, gpx_result *result);
+
+/* Reusable explorer: device memory (hash table, state store) is allocated once and
+ * each run resets it, so repeated explorations pay no allocation. */
+int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_explorer **out);
+int gpx_explorer_run(gpx_explorer *ex, gpx_result *result);
+/* Replace the model of an explorer (host gpf integers, copied to the device by this
+ * call); the new model must fit the explorer's key width. */
+int gpx_explorer_set_model(gpx_explorer *ex, const gpx_model *model);
+void gpx_explorer_destroy(gpx_explorer *ex);
+
+void gpx_result_free(gpx_result *result);
+
+/* Write the visited set of the last run in the reference's --dump format
+ * (print_local_queue, GPUexplore.cu:594-612): one state per line, local states
+ * comma separated, then the stripped state-vector words. */
+int gpx_explorer_dump(gpx_explorer *ex, const char *path);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPX_H */

@@ -1,0 +1,160 @@
+"""An independent BFS over the generators' abstract networks (test helper).
+
+It works on :class:`gpuexplore_gb300.gpf.Network` objects directly -- tuples of
+local states, Python dicts -- and never touches the gpf encoding, so agreement
+with the C oracle (which decodes gpf bit fields) pins the encoder, the oracle's
+decoder and its successor relation at once.  It restates the same semantics as
+the oracle (GPUexplore.cu:904-1122 successors, 1134-1151 deadlock, 927-935 and
+1063-1069 safety, 1345-1675 cluster POR with the cycle proviso evaluated
+against the visited set at the start of the level).  Small models only.
+"""
+from __future__ import annotations
+
+from itertools import product
+from typing import Dict, List, Optional, Set, Tuple
+
+from gpuexplore_gb300.gpf import Network
+
+State = Tuple[int, ...]
+
+
+def successors(net: Network, s: State) -> List[Tuple[State, int]]:
+    """All successors of s with their origin mask (1<<p for a local move of p,
+    the rule mask for a synchronisation)."""
+    n = net.nprocs
+    out: List[Tuple[State, int]] = []
+    for p in range(n):
+        for t in net.local[p][s[p]]:
+            v = list(s)
+            v[p] = t
+            out.append((tuple(v), 1 << p))
+    actions = set()
+    for p in range(n):
+        actions.update(net.sync[p][s[p]])
+    for a in sorted(actions):
+        enabled = {p for p in range(n) if a in net.sync[p][s[p]]}
+        for r in net.rules.get(a, []):
+            parts = [p for p in range(n) if r >> p & 1]
+            if not set(parts) <= enabled:
+                continue
+            for combo in product(*[net.sync[p][s[p]][a] for p in parts]):
+                v = list(s)
+                for p, t in zip(parts, combo):
+                    v[p] = t
+                out.append((tuple(v), r))
+    return out
+
+
+def static_clusters(net: Network, s: State) -> List[int]:
+    n = net.nprocs
+    cl = []
+    for p in range(n):
+        c = 1 << p
+        for a in net.sync[p][s[p]]:
+            for r in net.rules.get(a, []):
+                if r >> p & 1:
+                    c |= r
+        cl.append(c)
+    return cl
+
+
+def select_cluster(n: int, cl: List[int], prov: int) -> int:
+    c = [cl[p] if prov >> p & 1 else cl[p] & ~(1 << p) for p in range(n)]
+    best, bestc = (1 << n) - 1, n
+    for p in range(n):
+        closure = c[p]
+        stack = [i for i in range(n) if c[p] >> i & 1]
+        seen = set(stack)
+        while stack:
+            i = stack.pop()
+            closure |= c[i]
+            for j in range(n):
+                if c[i] >> j & 1 and j not in seen:
+                    seen.add(j)
+                    stack.append(j)
+        valid = any(c[i] >> i & 1 for i in range(n) if closure >> i & 1)
+        if valid and closure and bin(closure).count("1") < bestc:
+            bestc, best = bin(closure).count("1"), closure
+    return best
+
+
+def explore(net: Network, prop: str = "none", por: bool = False, proviso: bool = False,
+            max_states: int = 0) -> Dict:
+    n = net.nprocs
+    init: State = tuple([0] * n)
+    visited: Set[State] = {init}
+    frontier = [init]
+    levels = [1]
+    verdict = "none"
+    stopped = "done"
+    while frontier:
+        violation = False
+        nxt: List[State] = []
+        decisions: Dict[State, int] = {}
+        for s in frontier:
+            succ = successors(net, s)
+            if prop == "deadlock" and not succ:
+                violation = True
+            if prop == "safety" and any(t[n - 1] == 1 for t, _ in succ):
+                violation = True
+            sel = (1 << n) - 1
+            if por:
+                prov = 0
+                for t, mask in succ:
+                    if not proviso or t not in visited:
+                        prov |= mask
+                sel = select_cluster(n, static_clusters(net, s), prov)
+            decisions[s] = sel
+        for s in frontier:
+            sel = decisions[s]
+            for t, mask in successors(net, s):
+                if mask & sel == mask and t not in visited:
+                    visited.add(t)
+                    nxt.append(t)
+        if nxt:
+            levels.append(len(nxt))
+        frontier = nxt
+        if violation:
+            verdict = prop
+            stopped = "violation"
+            break
+        if max_states and len(visited) >= max_states and frontier:
+            stopped = "budget"
+            break
+    return {"states": len(visited), "levels": levels, "verdict": verdict, "stopped": stopped,
+            "visited": visited}
+
+
+def pack(net: Network, s: State) -> List[int]:
+    """Pack a state tuple into gpf state-vector words (firstbit layout)."""
+    fb = net.firstbit()
+    W = max(1, (fb[-1] + 31) // 32)
+    x = 0
+    for p, v in enumerate(s):
+        x |= v << fb[p]
+    return [(x >> (32 * i)) & 0xFFFFFFFF for i in range(W)]
+
+
+MASK64 = (1 << 64) - 1
+
+
+def _mix64(z: int) -> int:
+    z = (z + 0x9E3779B97F4A7C15) & MASK64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & MASK64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & MASK64
+    return z ^ (z >> 31)
+
+
+def key_hash(words: List[int]) -> int:
+    h = 0x9E3779B97F4A7C15
+    for j in range(0, len(words), 2):
+        c = words[j] | ((words[j + 1] << 32) if j + 1 < len(words) else 0)
+        h = _mix64(h ^ c)
+    return h
+
+
+def set_hash(net: Network, states: Optional[Set[State]]) -> str:
+    total = 0
+    for s in states or ():
+        total = (total + key_hash(pack(net, s))) & MASK64
+    return f"{total:016x}"

@@ -1,0 +1,88 @@
+"""GPU parity: libgpx (CUDA, through the C ABI) against the CPU oracle.
+
+Bit-exact on every integer result: visited-state count, per-level counts,
+verdict, stop reason and the order-independent hash of the visited set; for
+small models the full visited set is compared row by row.
+"""
+import numpy as np
+import pytest
+
+from gpuexplore_gb300 import gen
+from helpers import FLAGS, oracle, write_net
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu(lib, path, kw, **extra):
+    args = dict(kw)
+    args.update(extra)
+    args.setdefault("q_words", 1 << 22)
+    return lib.explore(path, check=False, **args)
+
+
+def _same(o, g):
+    assert g["rc"] == 0, g
+    assert g["states"] == o["states"]
+    assert g["levels"] == o["levels"]
+    assert g["verdict"] == o["verdict"]
+    assert g["stopped"] == o["stopped"]
+    assert g["set_hash"] == o["set_hash"]
+
+
+MODELS = {
+    "ring1": lambda: gen.ring(1),
+    "ring2": lambda: gen.ring(2),
+    "ring7": lambda: gen.ring(7),
+    "rand6": lambda: gen.random_network(11, nprocs=6, states=(3, 6)),           # 32-bit keys
+    "rand12": lambda: gen.random_network(12, nprocs=12, states=(4, 9)),         # 64-bit keys
+    "rand24": lambda: gen.random_network(13, nprocs=24, states=(4, 9), outdeg=(1, 2)),  # 128-bit keys
+    "dead9": lambda: gen.random_network(16, nprocs=9, states=(3, 6), outdeg=(1, 2), sync_frac=0.7),
+    "clus10": lambda: gen.clustered(14, nprocs=10, nclusters=(3, 3)),
+    "clus16": lambda: gen.clustered(15, nprocs=16, nclusters=(4, 5), states=(3, 5)),
+}
+
+
+@pytest.mark.parametrize("model", sorted(MODELS))
+@pytest.mark.parametrize("flags", sorted(FLAGS))
+def test_parity(gpu, tmp_path, model, flags):
+    net = MODELS[model]()
+    path = write_net(net, tmp_path, model)
+    cli, kw = FLAGS[flags]
+    budget = 300_000
+    o = oracle(path, cli, max_states=budget)
+    g = _gpu(gpu, path, kw, max_states=budget, q_words=1 << 24)
+    _same(o, g)
+
+
+@pytest.mark.parametrize("launch", [dict(blocks=1, threads=32), dict(kernel_iters=1), dict(kernel_iters=3),
+                                    dict(blocks=7, threads=96)])
+def test_launch_shapes(gpu, tmp_path, launch):
+    net = gen.random_network(21, nprocs=9, states=(3, 7))
+    path = write_net(net, tmp_path, "shape")
+    for flags in ("deadlock", "por_proviso"):
+        cli, kw = FLAGS[flags]
+        o = oracle(path, cli, max_states=100_000)
+        g = _gpu(gpu, path, kw, max_states=100_000, **launch)
+        _same(o, g)
+        if launch.get("kernel_iters"):
+            assert g["launches"] >= (len(g["levels"]) - 1) // launch["kernel_iters"]  # one level per expansion
+
+
+def test_full_set_rows(gpu, tmp_path):
+    """The visited set row by row (sorted), not only its hash."""
+    net = gen.random_network(31, nprocs=10, states=(3, 6))
+    path = write_net(net, tmp_path, "rows")
+    dump = str(tmp_path / "oracle.bin")
+    o = oracle(path, [], dump=dump)
+    g = _gpu(gpu, path, {}, collect_states=1)
+    _same(o, g)
+    ref = np.fromfile(dump, dtype=np.uint32).reshape(-1, g["key_words"])
+    got = g["states_words"]
+    assert got.shape == ref.shape
+    srt = lambda a: a[np.lexsort(a.T[::-1])]  # noqa: E731
+    assert np.array_equal(srt(got), srt(ref))
+    # the store holds each state once, and the table holds exactly the stored states
+    assert len(np.unique(got, axis=0)) == len(got)
+    assert g["table_count"] == g["states"]
+    # BFS order: level boundaries of the store match the per-level counts
+    assert got.shape[0] == sum(g["levels"])
