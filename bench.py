@@ -1,0 +1,275 @@
+"""Benchmark: new states/s of on-the-fly exploration on one GB300 (per rank).
+
+Workload (the config-2 network): a seeded random gpf network of 16 processes
+with U[8, 32] local states, local out-degree U[1, 4], 20% of transitions
+synchronising 2-3 processes, plus the embedded safety monitor (17 processes,
+82-bit state vectors, 128-bit hash slots); deadlock check (-d); exploration to
+the end of the BFS level that reaches 1e8 states; hash table of 5e9 32-bit
+words (20 GB).  One step = one complete exploration: table reset, initial
+state, all levels.  Inputs are synthetic (seeded generator) -- the reference's
+model set is not available.
+
+value    states / device time of the step (table reset + exploration kernels,
+         CUDA events on the launching stream; the model is already resident)
+e2e      the same metric through the C ABI with host buffers: every step parses
+         the gpf words from host memory, copies the model to the device
+         (gpx_explorer_set_model) and reads the results back (gpx_explorer_run)
+roofline dominant kernel (explore_kernel): algorithmic bytes per launch --
+         32 B per hash lookup, 32 B per insert, 2 x 4*sv_nints B per expanded
+         state -- over its CUDA-event duration, against the measured HBM peak
+cpu_baseline / --impl reference
+         the CPU oracle (a port of the reference's semantics; the reference has
+         no CPU path) with all host threads, on the first 9 BFS levels of the
+         same network
+
+Multi-GPU (torchrun): replicas -- each rank explores its own copy; the job
+value is the sum of states over the max step time across ranks ("weak").
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 2024
+BUDGET = 100_000_000
+Q_WORDS = 5_000_000_000
+CPU_SAMPLE_BUDGET = 10_000_000  # stops after BFS level 8 (about 4.2e7 states)
+WORKLOAD = "config-2 random gpf network (16 procs + monitor, seed 2024), -d, BFS to 1e8-state budget"
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def make_network_words():
+    from gpuexplore_gb300 import gen, gpf
+    net = gen.random_network(SEED)
+    return net, gpf.encode(net)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(r, sv_nints):
+    """32 B per hash lookup (one DRAM sector), 32 B per insert (the sector written
+    back), and the frontier write + read of each expanded state."""
+    return 32 * r["lookups"] + 32 * r["inserts"] + 2 * 4 * sv_nints * r["expanded"]
+
+
+def cpu_oracle_run(path, threads, budget):
+    from gpuexplore_gb300.build import ORACLE
+    out = subprocess.run([ORACLE, path, "-d", "--threads", str(threads), "--max-states", str(budget)],
+                         capture_output=True, text=True, check=True)
+    return json.loads(out.stdout)
+
+
+def run_reference(args, rank, world):
+    """The CPU oracle (the reference's semantics on host cores) on a bounded sample."""
+    if rank != 0:
+        return
+    from gpuexplore_gb300 import build, gpf
+    build.build_oracle()
+    net, words = make_network_words()
+    threads = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "c2.gpf")
+        gpf.write(net, path)
+        for _ in range(args.warmup):
+            cpu_oracle_run(path, threads, CPU_SAMPLE_BUDGET)
+        secs, states = [], 0
+        for _ in range(args.steps):
+            o = cpu_oracle_run(path, threads, CPU_SAMPLE_BUDGET)
+            secs.append(o["seconds"])
+            states = o["states"]
+    v = states / (sum(secs) / len(secs))
+    sample = f"first {len(o['levels'])} BFS levels ({states} states) of the same network"
+    line = {"impl": "reference", "metric": "new states/s", "value": v, "unit": "states/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(secs) / len(secs),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": sample, "cpu_threads": threads},
+            "cpu_baseline": {"value": v, "unit": "states/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "states/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpx", choices=["gpx", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist = dist_mod
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    from gpuexplore_gb300 import build, lib
+    build.build_all()
+    net, words = make_network_words()
+    sv_nints = (net.firstbit()[-1] + 1 + 31) // 32  # the reference's words per vector
+    model = lib.Model.from_words(words)
+    opts = lib.options(property="deadlock", q_words=Q_WORDS, max_states=BUDGET, device=local)
+    ex = lib.Explorer(model, opts)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        ex.run()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    dev_ms, ker_ms, results = [], [], []
+    for _ in range(args.steps):
+        r = ex.run()
+        dev_ms.append(r["setup_ms"] + r["kernel_ms"])
+        ker_ms.append(r["kernel_ms"])
+        results.append(r)
+    # end to end through the C ABI from host buffers
+    e2e_s = []
+    h2d = len(words) * 4
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        m = lib.Model.from_words(words)
+        ex.set_model(m)
+        r2 = ex.run()
+        e2e_s.append(time.perf_counter() - t0)
+        m.close()
+    barrier()
+    clk = clocks.stop()
+    r = results[-1]
+    for x in results + [r2]:
+        assert x["states"] == r["states"] and x["levels"] == r["levels"] and x["set_hash"] == r["set_hash"]
+    step_ms = sum(dev_ms) / len(dev_ms)
+    e2e_step = sum(e2e_s) / len(e2e_s)
+    if dist:
+        import torch
+        t = torch.tensor([step_ms, e2e_step], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms, e2e_step = float(t[0]), float(t[1])
+    states_job = r["states"] * world
+    value = states_job / (step_ms / 1000.0)
+    e2e = states_job / e2e_step
+    abytes = algorithmic_bytes(r, sv_nints)
+    kms = sum(ker_ms) / len(ker_ms)
+    peaks, peak_kind = measured_peaks()
+    achieved = abytes / (kms / 1000.0) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "explore_kernel_config2.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            pj = json.load(f)
+        if pj.get("dram_bytes_per_state"):
+            traffic = pj["dram_bytes_per_state"] * r["states"]
+    line = {
+        "metric": "new states/s", "value": value, "unit": "states/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded gpf generator)",
+        "config": {"workload": WORKLOAD, "states": r["states"], "levels": len(r["levels"]),
+                   "table_gb": Q_WORDS * 4 / 1e9, "slot_bytes": r["slot_bytes"], "blocks": r["blocks"],
+                   "threads": r["threads"], "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (20 GB table, re-initialised every step)"},
+        "e2e": {"value": e2e, "unit": "states/s", "h2d_bytes_per_step": h2d + 160,
+                "d2h_bytes_per_step": 8 * len(r["levels"]) + 16 + 160},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                     "peak_source": f"{peak_kind} hbm_gbs", "kernel": "explore_kernel",
+                     "kernel_ms": kms, "algorithmic_bytes": abytes,
+                     "lookups": r["lookups"], "inserts": r["inserts"], "expanded": r["expanded"],
+                     "probes": r["probes"]},
+        "clocks": clk,
+        "gpu_launches": sum(x["launches"] + 2 for x in results),
+        "hash_probe_gbs": 32 * r["probes"] / (kms / 1000.0) / 1e9,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from gpuexplore_gb300 import gpf
+        threads = os.cpu_count() or 1
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "c2.gpf")
+            gpf.write(net, path)
+            o = cpu_oracle_run(path, threads, CPU_SAMPLE_BUDGET)
+        line["cpu_baseline"] = {"value": o["states"] / o["seconds"], "unit": "states/s", "cores": threads,
+                                "kind": "port",
+                                "sample": f"first {len(o['levels'])} BFS levels ({o['states']} states)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ex.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -58,7 +58,6 @@ namespace gpx {
 // ------------------------------------------------------------------ constants
 
 constexpr uint32_t kFull = 0xFFFFFFFFu;
-constexpr int kQcap = 64;       // per-warp successor queue (entries)
 constexpr int kPairMax = 256;   // (state, process) pairs staged per warp batch
 constexpr int kMaxProbe = 32;   // buckets probed before reporting the table full
 constexpr uint32_t kMaxLevels = 1u << 20;
@@ -196,7 +195,7 @@ template <> struct KT<K64> {
 // the middle of its insertion shows exactly one zero half ("torn"); such a slot
 // is re-read with an atomic before it is judged.
 template <> struct KT<K128> {
-    static constexpr int kSlots = 4; // 64-byte bucket
+    static constexpr int kSlots = 2; // 32-byte bucket
     static constexpr unsigned long long kOcc = 0x8000000000000000ull;
     __device__ static K128 initial() { return {kOcc, kOcc}; }
     __device__ static bool eq(const K128 &a, const K128 &b) { return a.lo == b.lo && a.hi == b.hi; }
@@ -238,14 +237,11 @@ template <> struct KT<K128> {
     }
     __device__ static void bucket(const K128 *b, K128 (&s)[kSlots]) {
         uint32_t w[8];
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            ld256_cg(b + 2 * h, w);
-            s[2 * h].lo = (unsigned long long)w[0] | ((unsigned long long)w[1] << 32);
-            s[2 * h].hi = (unsigned long long)w[2] | ((unsigned long long)w[3] << 32);
-            s[2 * h + 1].lo = (unsigned long long)w[4] | ((unsigned long long)w[5] << 32);
-            s[2 * h + 1].hi = (unsigned long long)w[6] | ((unsigned long long)w[7] << 32);
-        }
+        ld256_cg(b, w);
+        s[0].lo = (unsigned long long)w[0] | ((unsigned long long)w[1] << 32);
+        s[0].hi = (unsigned long long)w[2] | ((unsigned long long)w[3] << 32);
+        s[1].lo = (unsigned long long)w[4] | ((unsigned long long)w[5] << 32);
+        s[1].hi = (unsigned long long)w[6] | ((unsigned long long)w[7] << 32);
     }
     __device__ static K128 load(const K128 *p) {
         return {__ldcg(&p->lo), __ldcg(&p->hi)};
@@ -259,9 +255,14 @@ template <> struct KT<K128> {
     }
 };
 
+// Probe sequence of a key: 32-byte buckets visited in pairs -- a bucket, then
+// its neighbour in the same 64-byte line -- for kMaxProbe/2 hash functions.
+// The table holds an even number of buckets.
 __device__ __forceinline__ unsigned long long bucket_of(uint64_t h, int i, unsigned long long nb) {
-    uint64_t x = i ? mix64(h + (uint64_t)i * 0x9E3779B97F4A7C15ull) : h;
-    return __umul64hi(x, nb);
+    int j = i >> 1;
+    uint64_t x = j ? mix64(h + (uint64_t)j * 0x9E3779B97F4A7C15ull) : h;
+    unsigned long long b = __umul64hi(x, nb);
+    return (i & 1) ? (b ^ 1ull) : b;
 }
 
 // Find-or-insert.  Returns 0 if the key was present, 1 if this call inserted
@@ -323,14 +324,18 @@ __device__ __forceinline__ bool find_key(K *table, unsigned long long nb, const 
 
 // --------------------------------------------------------- per-warp scratch
 
-template <class K> struct WarpScratch {
-    K keys[32];                 // the batch's source states
-    uint32_t appl[kPairMax];    // per pair: applicable rules among those it leads (bit r)
-    uint32_t cl0[kPairMax];     // per pair: static POR cluster
-    uint32_t clo[kPairMax];     // per pair: cluster closure
-    uint32_t en[32], prov[32], sel[32], best[32];
-    K qkey[kQcap];              // successor queue
-    uint32_t qg[kQcap], qmask[kQcap];
+constexpr int kStage = 64; // new states staged per warp before one store append
+
+template <class K, int MODE> struct WarpScratch {
+    static constexpr int kPor = (MODE == MODE_PLAIN) ? 1 : kPairMax;
+    K keys[32];                  // the batch's source states
+    K stage[kStage];             // new states waiting to be appended to the store
+    uint32_t appl[kPairMax];     // per pair: applicable rules among those it leads (bit r)
+    uint32_t pre[kPairMax + 1];  // per pair: successor count, then its exclusive prefix sum
+    uint32_t en[32];             // per state: some transition enabled
+    uint32_t cl0[kPor];          // per pair: static POR cluster
+    uint32_t clo[kPor];          // per pair: cluster closure
+    uint32_t prov[32], sel[32], best[32];
 };
 
 struct WarpStats {
@@ -451,61 +456,53 @@ template <int MODE> __device__ void grid_barrier(const Params &P) {
 template <class K, int MODE> struct Explorer {
     const Params &P;
     MView M;
-    WarpScratch<K> &ws;
+    WarpScratch<K, MODE> &ws;
     K *table;
     K *store;
     uint32_t lane;
     uint32_t lanemask_lt;
+    uint32_t shead, scount; // staged new states (warp-uniform)
     WarpStats st;
     bool safety, deadlock;
 
-    __device__ Explorer(const Params &p, const uint32_t *model, WarpScratch<K> &w)
+    __device__ Explorer(const Params &p, const uint32_t *model, WarpScratch<K, MODE> &w)
         : P(p), ws(w), table((K *)p.table), store((K *)p.store) {
         M.w = model;
         M.n = model[H_NPROCS];
         lane = threadIdx.x & 31;
         lanemask_lt = (1u << lane) - 1u;
+        shead = scount = 0;
         st = WarpStats{0, 0, 0, 0, 0, 0};
         safety = P.property == GPX_PROP_SAFETY;
         deadlock = P.property == GPX_PROP_DEADLOCK;
     }
 
-    // Drain `cnt` (<= 32) queue entries starting at `head`: one lookup per lane.
-    __device__ void drain(uint32_t head, uint32_t cnt, bool lookup_mode) {
-        bool valid = lane < cnt;
-        uint32_t pos = (head + lane) % kQcap;
-        int res = -1;
-        K key;
-        if (valid) {
-            key = ws.qkey[pos];
-            uint64_t h = KT<K>::hash(key, P.seed);
-            if (lookup_mode) {
-                bool found = find_key<K>(table, P.nbuckets, key, h, st.probes);
-                // cycle proviso: a successor satisfies it unless it is an explored
-                // ("OLD") state -- every state in the table during this pass
-                if (!found) atomicOr(&ws.prov[ws.qg[pos]], ws.qmask[pos]);
-            } else {
-                res = find_or_insert<K>(table, P.nbuckets, key, h, st.probes);
-                if (res == 2) set_error(P.ctrl, GPX_ERR_TABLE_FULL);
-            }
+    // Successors of rule k from `key`: the product of the participants' targets.
+    __device__ uint32_t product_size(const K &key, uint32_t mask, uint32_t act) const {
+        uint32_t psz = 1, rest = mask;
+        while (rest) {
+            uint32_t q = __ffs(rest) - 1;
+            rest &= rest - 1;
+            psz *= M.group(M.rec(q, KT<K>::get(key, M.fb(q), M.bs(q))), act)[2];
         }
-        st.lookups += cnt;
-        if (lookup_mode) return;
-        st.ilookups += cnt;
-        uint32_t ins = __ballot_sync(kFull, res == 1);
-        if (ins) {
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(&P.ctrl->store_count, (unsigned long long)__popc(ins));
-            base = __shfl_sync(kFull, base, 0);
-            if (res == 1) {
-                unsigned long long idx = base + __popc(ins & lanemask_lt);
-                if (idx < P.store_cap)
-                    store[idx] = key;
-                else
-                    set_error(P.ctrl, GPX_ERR_STORE_FULL);
-            }
-            st.inserts += __popc(ins);
+        return psz;
+    }
+
+    // Append `cnt` (<= 32) staged new states to the store with one atomic.
+    __device__ void stage_flush(uint32_t cnt) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(&P.ctrl->store_count, (unsigned long long)cnt);
+        base = __shfl_sync(kFull, base, 0);
+        if (lane < cnt) {
+            unsigned long long idx = base + lane;
+            if (idx < P.store_cap)
+                store[idx] = ws.stage[(shead + lane) % kStage];
+            else
+                set_error(P.ctrl, GPX_ERR_STORE_FULL);
         }
+        shead = (shead + cnt) % kStage;
+        scount -= cnt;
+        __syncwarp();
     }
 
     // Expand a batch of B states store[first .. first+B).
@@ -521,21 +518,23 @@ template <class K, int MODE> struct Explorer {
         __syncwarp();
         const uint32_t npairs = B * n;
         const bool check = (MODE != MODE_PROVISO) || decide;
+        const bool filter = (MODE == MODE_POR) || (MODE == MODE_PROVISO && !decide);
 
-        // A: enabledness, applicable rules, static clusters, safety on moves into monitor state 1
+        // A: enabledness, applicable rules, successor counts, static clusters,
+        //    safety on moves into monitor state 1 (GPUexplore.cu:927-935, 1063-1069)
         for (uint32_t i = lane; i < npairs; i += 32) {
             uint32_t g = i / n, p = i - g * n;
             K key = ws.keys[g];
             uint32_t s = KT<K>::get(key, M.fb(p), M.bs(p));
             const uint32_t *rec = M.rec(p, s);
             uint32_t lcnt = rec[R_LCNT], roff = rec[R_ROFF], rcnt = rec[R_RCNT];
-            uint32_t appl = 0, provbits = lcnt ? (1u << p) : 0u;
+            uint32_t appl = 0, provbits = lcnt ? (1u << p) : 0u, cnt = lcnt;
             bool viol = safety && check && p == n - 1 && (rec[R_FLAGS] & 1u);
             for (uint32_t r = 0; r < rcnt; r++) {
                 uint32_t k = M.lrule(roff + r);
                 uint32_t mask = M.rmask(k), act = M.ract(k);
                 bool ok = true, hit1 = false;
-                uint32_t rest = mask;
+                uint32_t rest = mask, psz = 1;
                 while (rest) {
                     uint32_t q = __ffs(rest) - 1;
                     rest &= rest - 1;
@@ -545,15 +544,18 @@ template <class K, int MODE> struct Explorer {
                         ok = false;
                         break;
                     }
+                    psz *= grp[2];
                     if (q == n - 1 && grp[3]) hit1 = true;
                 }
                 if (ok) {
                     appl |= 1u << r;
                     provbits |= mask;
+                    cnt += psz;
                     if (safety && check && hit1) viol = true;
                 }
             }
             ws.appl[i] = appl;
+            ws.pre[i] = cnt;
             if (MODE != MODE_PLAIN) ws.cl0[i] = rec[R_CL0];
             if (lcnt | appl) ws.en[g] = 1;
             if (MODE == MODE_POR) atomicOr(&ws.prov[g], provbits);
@@ -563,17 +565,132 @@ template <class K, int MODE> struct Explorer {
         if (deadlock && check && lane < B && ws.en[lane] == 0) st.violation = 1;
         if (check && lane < B) st.expanded++;
 
-        // B: cluster selection (POR without cycle proviso, from enabledness)
+        // B: the cluster each state expands (POR); without the cycle proviso the
+        //    proviso bits are plain enabledness (GPUexplore.cu:1395-1397)
         if (MODE == MODE_POR) select_clusters(B);
         if (MODE == MODE_PROVISO && !decide) {
             if (lane < B) ws.sel[lane] = __ldcg(P.sel + lvl_off + lane);
             __syncwarp();
         }
+        if (filter) {
+            // successors of transitions inside the cluster only (GPUexplore.cu:1409, 1541)
+            for (uint32_t i = lane; i < npairs; i += 32) {
+                uint32_t g = i / n, p = i - g * n;
+                uint32_t sel = ws.sel[g];
+                K key = ws.keys[g];
+                const uint32_t *rec = M.rec(p, KT<K>::get(key, M.fb(p), M.bs(p)));
+                uint32_t cnt = (sel >> p & 1u) ? rec[R_LCNT] : 0u;
+                uint32_t a = ws.appl[i], keep = 0, roff = rec[R_ROFF];
+                while (a) {
+                    uint32_t r = __ffs(a) - 1;
+                    a &= a - 1;
+                    uint32_t k = M.lrule(roff + r), mask = M.rmask(k);
+                    if ((mask & sel) != mask) continue;
+                    keep |= 1u << r;
+                    cnt += product_size(key, mask, M.ract(k));
+                }
+                ws.appl[i] = keep;
+                ws.pre[i] = cnt;
+            }
+            __syncwarp();
+        }
 
-        // C: emit successors (all of them when deciding, else those of the selected cluster)
-        emit(B, decide);
+        // exclusive prefix sum of the per-pair successor counts
+        uint32_t carry = 0;
+        for (uint32_t base = 0; base < npairs; base += 32) {
+            uint32_t i = base + lane;
+            uint32_t v = i < npairs ? ws.pre[i] : 0u, incl = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(kFull, incl, o);
+                if (lane >= (uint32_t)o) incl += y;
+            }
+            if (i < npairs) ws.pre[i] = carry + incl - v;
+            carry += __shfl_sync(kFull, incl, 31);
+        }
+        if (lane == 0) ws.pre[npairs] = carry;
+        __syncwarp();
+
+        // C: one successor per lane per round, materialised by index, then looked up
+        for (uint32_t t0 = 0; t0 < carry; t0 += 32) {
+            uint32_t t = t0 + lane;
+            bool valid = t < carry;
+            K out;
+            uint32_t og = 0, omask = 0;
+            if (valid) {
+                uint32_t lo = 0, hi = npairs;
+                while (hi - lo > 1) {
+                    uint32_t mid = (lo + hi) >> 1;
+                    if (ws.pre[mid] <= t) lo = mid;
+                    else hi = mid;
+                }
+                uint32_t sub = t - ws.pre[lo];
+                og = lo / n;
+                uint32_t p = lo - og * n;
+                K key = ws.keys[og];
+                const uint32_t *rec = M.rec(p, KT<K>::get(key, M.fb(p), M.bs(p)));
+                uint32_t lcnt = (!filter || (ws.sel[og] >> p & 1u)) ? rec[R_LCNT] : 0u;
+                out = key;
+                if (sub < lcnt) {
+                    KT<K>::set(out, M.fb(p), M.bs(p), M.ltgt(rec[R_LOFF] + sub));
+                    omask = 1u << p;
+                } else {
+                    sub -= lcnt;
+                    uint32_t a = ws.appl[lo], roff = rec[R_ROFF];
+                    while (a) {
+                        uint32_t r = __ffs(a) - 1;
+                        a &= a - 1;
+                        uint32_t k = M.lrule(roff + r), mask = M.rmask(k), act = M.ract(k);
+                        uint32_t psz = product_size(key, mask, act);
+                        if (sub >= psz) {
+                            sub -= psz;
+                            continue;
+                        }
+                        uint32_t rest = mask;
+                        while (rest) {
+                            uint32_t q = __ffs(rest) - 1;
+                            rest &= rest - 1;
+                            const uint32_t *grp = M.group(M.rec(q, KT<K>::get(key, M.fb(q), M.bs(q))), act);
+                            uint32_t tc = grp[2], d = sub % tc;
+                            sub /= tc;
+                            KT<K>::set(out, M.fb(q), M.bs(q), M.stgt(grp[1] + d));
+                        }
+                        omask = mask;
+                        break;
+                    }
+                }
+            }
+            if (MODE == MODE_PROVISO && decide) {
+                if (valid) {
+                    st.lookups++;
+                    // cycle proviso: a successor satisfies it unless it is an explored
+                    // ("OLD") state -- every state in the table during this pass
+                    if (!find_key<K>(table, P.nbuckets, out, KT<K>::hash(out, P.seed), st.probes))
+                        atomicOr(&ws.prov[og], omask);
+                }
+                continue;
+            }
+            int res = -1;
+            if (valid) {
+                st.lookups++;
+                st.ilookups++;
+                res = find_or_insert<K>(table, P.nbuckets, out, KT<K>::hash(out, P.seed), st.probes);
+                if (res == 2) set_error(P.ctrl, GPX_ERR_TABLE_FULL);
+            }
+            uint32_t ins = __ballot_sync(kFull, res == 1);
+            if (ins) {
+                if (res == 1) {
+                    ws.stage[(shead + scount + __popc(ins & lanemask_lt)) % kStage] = out;
+                    st.inserts++;
+                }
+                scount += __popc(ins);
+                __syncwarp();
+                if (scount >= 32) stage_flush(32);
+            }
+        }
 
         if (MODE == MODE_PROVISO && decide) {
+            __syncwarp();
             select_clusters(B);
             if (lane < B) P.sel[lvl_off + lane] = ws.sel[lane];
         }
@@ -583,6 +700,7 @@ template <class K, int MODE> struct Explorer {
     // Smallest valid cluster per state (GPUexplore.cu:1633-1672); ws.prov holds
     // the proviso bits, ws.cl0 the static clusters.
     __device__ void select_clusters(uint32_t B) {
+        if (MODE == MODE_PLAIN) return;
         const uint32_t n = M.n;
         __syncwarp();
         const uint32_t npairs = B * n;
@@ -612,125 +730,8 @@ template <class K, int MODE> struct Explorer {
         __syncwarp();
     }
 
-    __device__ void emit(uint32_t B, bool decide) {
-        const uint32_t n = M.n;
-        const uint32_t npairs = B * n;
-        const bool filter = (MODE != MODE_PLAIN) && !decide;
-        uint32_t pair = lane;
-        int stage = 0;
-        uint32_t g = 0, p = 0, j = 0, lcnt = 0, loff = 0, arem = 0, roff = 0;
-        uint32_t rmask = 0, ract = 0, pidx = 0, psize = 0;
-        K key;
-        memset(&key, 0, sizeof key);
-        uint32_t head = 0, count = 0;
-        for (;;) {
-            bool have = false;
-            K out;
-            uint32_t omask = 0;
-            while (!have && stage != 3) {
-                if (stage == 0) {
-                    if (pair >= npairs) {
-                        stage = 3;
-                        break;
-                    }
-                    g = pair / n;
-                    p = pair - g * n;
-                    key = ws.keys[g];
-                    uint32_t s = KT<K>::get(key, M.fb(p), M.bs(p));
-                    const uint32_t *rec = M.rec(p, s);
-                    uint32_t sel = filter ? ws.sel[g] : kFull;
-                    lcnt = (sel >> p & 1u) ? rec[R_LCNT] : 0u;
-                    loff = rec[R_LOFF];
-                    roff = rec[R_ROFF];
-                    arem = ws.appl[pair];
-                    if (filter) {
-                        uint32_t a = arem;
-                        while (a) {
-                            uint32_t r = __ffs(a) - 1;
-                            a &= a - 1;
-                            uint32_t m = M.rmask(M.lrule(roff + r));
-                            if ((m & sel) != m) arem &= ~(1u << r);
-                        }
-                    }
-                    j = 0;
-                    pidx = psize = 0;
-                    stage = 1;
-                }
-                if (stage == 1) {
-                    if (j < lcnt) {
-                        out = key;
-                        KT<K>::set(out, M.fb(p), M.bs(p), M.ltgt(loff + j));
-                        j++;
-                        omask = 1u << p;
-                        have = true;
-                        break;
-                    }
-                    stage = 2;
-                }
-                if (stage == 2) {
-                    if (pidx < psize) {
-                        out = key;
-                        uint32_t idx = pidx, rest = rmask;
-                        while (rest) {
-                            uint32_t q = __ffs(rest) - 1;
-                            rest &= rest - 1;
-                            uint32_t sq = KT<K>::get(key, M.fb(q), M.bs(q));
-                            const uint32_t *grp = M.group(M.rec(q, sq), ract);
-                            uint32_t tc = grp[2];
-                            uint32_t d = idx % tc;
-                            idx /= tc;
-                            KT<K>::set(out, M.fb(q), M.bs(q), M.stgt(grp[1] + d));
-                        }
-                        pidx++;
-                        omask = rmask;
-                        have = true;
-                        break;
-                    }
-                    if (arem == 0) {
-                        stage = 0;
-                        pair += 32;
-                        continue;
-                    }
-                    uint32_t r = __ffs(arem) - 1;
-                    arem &= arem - 1;
-                    uint32_t k = M.lrule(roff + r);
-                    rmask = M.rmask(k);
-                    ract = M.ract(k);
-                    psize = 1;
-                    uint32_t rest = rmask;
-                    while (rest) {
-                        uint32_t q = __ffs(rest) - 1;
-                        rest &= rest - 1;
-                        uint32_t sq = KT<K>::get(key, M.fb(q), M.bs(q));
-                        psize *= M.group(M.rec(q, sq), ract)[2];
-                    }
-                    pidx = 0;
-                }
-            }
-            uint32_t bal = __ballot_sync(kFull, have);
-            if (!bal) break;
-            if (have) {
-                uint32_t pos = (head + count + __popc(bal & lanemask_lt)) % kQcap;
-                ws.qkey[pos] = out;
-                ws.qg[pos] = g;
-                ws.qmask[pos] = omask;
-            }
-            count += __popc(bal);
-            __syncwarp();
-            if (count >= 32) {
-                drain(head, 32, decide);
-                head = (head + 32) % kQcap;
-                count -= 32;
-                __syncwarp();
-            }
-        }
-        if (count) {
-            drain(head, count, decide);
-            __syncwarp();
-        }
-    }
-
     __device__ void flush_stats() {
+        if (scount) stage_flush(scount);
         Ctrl *c = P.ctrl;
         unsigned int v[5] = {st.lookups, st.probes, st.inserts, st.expanded, st.ilookups};
 #pragma unroll
@@ -749,7 +750,7 @@ template <class K, int MODE> struct Explorer {
     }
 };
 
-template <class K, int MODE> __global__ void __launch_bounds__(256) explore_kernel(Params P) {
+template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_kernel(Params P) {
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t *model = P.model;
     size_t model_bytes = 0;
@@ -759,8 +760,8 @@ template <class K, int MODE> __global__ void __launch_bounds__(256) explore_kern
         model = m;
         model_bytes = ((size_t)P.model_words * 4 + 127) & ~(size_t)127;
     }
-    WarpScratch<K> *wsall = (WarpScratch<K> *)(smem + model_bytes);
-    WarpScratch<K> &ws = wsall[threadIdx.x >> 5];
+    WarpScratch<K, MODE> *wsall = (WarpScratch<K, MODE> *)(smem + model_bytes);
+    WarpScratch<K, MODE> &ws = wsall[threadIdx.x >> 5];
     __syncthreads();
 
     Explorer<K, MODE> E(P, model, ws);
@@ -868,7 +869,7 @@ const char *kStatusStrings[] = {"ok",
 struct KernelSet {
     void (*explore[3])(Params);
     void (*init)(Params);
-    size_t scratch_bytes;
+    size_t scratch_bytes[3];
     uint32_t slot_bytes, bucket_slots;
 };
 
@@ -878,7 +879,9 @@ template <class K> KernelSet kernels_for() {
     s.explore[1] = explore_kernel<K, MODE_POR>;
     s.explore[2] = explore_kernel<K, MODE_PROVISO>;
     s.init = init_kernel<K>;
-    s.scratch_bytes = sizeof(WarpScratch<K>);
+    s.scratch_bytes[0] = sizeof(WarpScratch<K, MODE_PLAIN>);
+    s.scratch_bytes[1] = sizeof(WarpScratch<K, MODE_POR>);
+    s.scratch_bytes[2] = sizeof(WarpScratch<K, MODE_PROVISO>);
     s.slot_bytes = sizeof(K);
     s.bucket_slots = KT<K>::kSlots;
     return s;
@@ -955,7 +958,7 @@ int configure_launch(gpx_explorer *ex) {
     int threads = ex->o.threads > 0 ? ex->o.threads : 256;
     if (threads % 32 || threads > 256) return GPX_ERR_INVALID;
     const size_t smem_limit = ex->prop.sharedMemPerBlockOptin;
-    size_t scratch = (size_t)(threads / 32) * ex->ks.scratch_bytes;
+    size_t scratch = (size_t)(threads / 32) * ex->ks.scratch_bytes[ex->mode];
     size_t mb = (model_bytes + 127) & ~(size_t)127;
     ex->model_in_smem = (mb + scratch <= smem_limit) && model_bytes <= 96 * 1024;
     ex->smem = scratch + (ex->model_in_smem ? mb : 0);
@@ -1179,8 +1182,8 @@ int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_exp
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return fail(GPX_ERR_CUDA);
     const size_t bucket_bytes = (size_t)ex->ks.slot_bytes * ex->ks.bucket_slots;
     size_t tb = opts->q_words ? (size_t)opts->q_words * 4 : free_b / 4;
-    tb = (tb / bucket_bytes) * bucket_bytes;
-    if (tb < bucket_bytes) return fail(GPX_ERR_INVALID);
+    tb = (tb / (2 * bucket_bytes)) * (2 * bucket_bytes); // buckets are probed in pairs
+    if (tb < 2 * bucket_bytes) return fail(GPX_ERR_INVALID);
     ex->table_bytes = tb;
     ex->nbuckets = tb / bucket_bytes;
     ex->slots = ex->nbuckets * ex->ks.bucket_slots;
@@ -1289,6 +1292,7 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     r->lookups = c.lookups;
     r->transitions = c.inserts_lookups; // successors sent to the table for insertion
     r->probes = c.probes;
+    r->inserts = c.inserts;
     r->expanded = c.expanded;
     r->launches = launches;
     r->kernel_ms = kernel_ms;

@@ -99,6 +99,7 @@ typedef struct {
     uint64_t table_slots;    /* hash-table capacity in states */
     uint32_t slot_bytes;     /* bytes per hash-table slot (4, 8 or 16) */
     uint32_t blocks, threads;/* launch configuration that ran */
+    uint64_t inserts;        /* states inserted into the hash table by the exploration kernels */
 } gpx_result;
 
 typedef struct gpx_model gpx_model;
