@@ -41,6 +41,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -1387,3 +1388,205 @@ int gpx_explorer_dump(gpx_explorer *ex, const char *path) {
 }
 
 } // extern "C"
+
+// ======================================================= allocation-free entry point
+//
+// gpx_explore_noalloc runs the same kernels as gpx_explore with every piece of
+// device scratch -- control block, set-hash scalars, level counts, model,
+// hash table, state store, cluster array -- carved out of one static device
+// array, so the call allocates nothing.  Layout (byte offsets):
+//   [0, 256)            Ctrl
+//   [256, 320)          set-hash / table-count scalars
+//   [4096, +8 MiB)      level counts (kMaxLevels entries)
+//   then                model words, hash table, state store, cluster array
+static __device__ __align__(256) unsigned char g_gpx_noalloc_scratch[GPX_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kNoallocMaxDevices = 256;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_base[kNoallocMaxDevices] = {nullptr};
+
+// Device address of the static array on `device` (current), looked up once per device.
+int noalloc_base(int device, unsigned char **out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (device < 0 || device >= kNoallocMaxDevices) return GPX_ERR_INVALID;
+    if (!g_noalloc_base[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_gpx_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            fprintf(stderr, "gpx_explore_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+            return GPX_ERR_CUDA;
+        }
+        g_noalloc_base[device] = p;
+    }
+    *out = (unsigned char *)g_noalloc_base[device];
+    return GPX_OK;
+}
+
+size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+} // namespace
+
+extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *opts, uint64_t *level_counts,
+                                   uint32_t level_capacity, gpx_result *r) {
+    if (!model || !opts || !r || opts->struct_size != sizeof(gpx_options)) return GPX_ERR_INVALID;
+    if (!level_counts && level_capacity) return GPX_ERR_INVALID;
+    memset(r, 0, sizeof *r);
+    r->struct_size = sizeof *r;
+    auto t_start = std::chrono::steady_clock::now();
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPX_ERR_NO_GPU;
+    if (opts->device < 0 || opts->device >= ndev) return GPX_ERR_INVALID;
+    GPX_CUDA(cudaSetDevice(opts->device));
+    unsigned char *base = nullptr;
+    int rc = noalloc_base(opts->device, &base);
+    if (rc != GPX_OK) return rc;
+
+    const int mode = opts->por ? (opts->cycle_proviso ? MODE_PROVISO : MODE_POR) : MODE_PLAIN;
+    int property = opts->property;
+    if (property == GPX_PROP_SAFETY && model->gpf.liveness == 1) property = GPX_PROP_LIVENESS;
+    const int kind = select_kind(model->dec.state_bits);
+    KernelSet ks = kind == 0 ? kernels_for<K32>() : (kind == 1 ? kernels_for<K64>() : kernels_for<K128>());
+
+    // carve the array
+    const size_t total = GPX_NOALLOC_SCRATCH_BYTES;
+    const size_t off_ctrl = 0, off_scalar = 256, off_levels = 4096;
+    const size_t off_model = round_up(off_levels + (size_t)kMaxLevels * 8, 256);
+    const size_t model_bytes = model->dec.words.size() * 4;
+    const size_t off_table = round_up(off_model + model_bytes, 256);
+    if (off_table >= total) {
+        fprintf(stderr, "gpx_explore_noalloc: model of %zu bytes does not fit in the %zu-byte scratch array\n",
+                model_bytes, total);
+        return GPX_ERR_INVALID;
+    }
+    const size_t bucket_bytes = (size_t)ks.slot_bytes * ks.bucket_slots;
+    const size_t per_state = ks.slot_bytes + (mode == MODE_PROVISO ? 4 : 0);
+    size_t left = total - off_table;
+    size_t tb = opts->q_words ? (size_t)opts->q_words * 4 : left / 2;
+    tb = tb / (2 * bucket_bytes) * (2 * bucket_bytes);
+    // the store and the cluster array each start on a 256-byte boundary
+    size_t cap = opts->store_states ? (size_t)opts->store_states : (left > tb + 512 ? (left - tb - 512) / per_state : 0);
+    if (tb < 2 * bucket_bytes || cap < 1 || tb + cap * per_state + 512 > left) {
+        fprintf(stderr,
+                "gpx_explore_noalloc: requested %zu table bytes + %zu states x %zu bytes, but only %zu bytes of the "
+                "%zu-byte scratch array are left after the control block, level counts and model\n",
+                tb, cap, per_state, left, total);
+        return GPX_ERR_INVALID;
+    }
+    const size_t off_store = off_table + tb;
+    const size_t off_sel = round_up(off_store + cap * ks.slot_bytes, 256);
+    if (mode == MODE_PROVISO && off_sel + cap * 4 > total) {
+        fprintf(stderr, "gpx_explore_noalloc: the cluster array does not fit in the scratch array\n");
+        return GPX_ERR_INVALID;
+    }
+
+    // launch shape (no allocation: attributes and occupancy queries only)
+    cudaDeviceProp prop;
+    GPX_CUDA(cudaGetDeviceProperties(&prop, opts->device));
+    int threads = opts->threads > 0 ? opts->threads : 256;
+    if (threads % 32 || threads > 256) return GPX_ERR_INVALID;
+    size_t scratch = (size_t)(threads / 32) * ks.scratch_bytes[mode];
+    size_t mb = (model_bytes + 127) & ~(size_t)127;
+    bool in_smem = (mb + scratch <= prop.sharedMemPerBlockOptin) && model_bytes <= 96 * 1024;
+    size_t smem = scratch + (in_smem ? mb : 0);
+    if (smem > prop.sharedMemPerBlockOptin) return GPX_ERR_UNSUPPORTED;
+    GPX_CUDA(cudaFuncSetAttribute((const void *)ks.explore[mode], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    int per_sm = 0;
+    GPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)ks.explore[mode], threads, smem));
+    if (per_sm < 1) return GPX_ERR_UNSUPPORTED;
+    int max_blocks = per_sm * prop.multiProcessorCount;
+    int blocks = std::max(1, opts->blocks > 0 ? std::min(opts->blocks, max_blocks) : max_blocks);
+
+    Ctrl *d_ctrl = (Ctrl *)(base + off_ctrl);
+    unsigned long long *d_scalar = (unsigned long long *)(base + off_scalar);
+    Params P;
+    memset(&P, 0, sizeof P);
+    P.table = base + off_table;
+    P.nbuckets = tb / bucket_bytes;
+    P.store = base + off_store;
+    P.store_cap = cap;
+    P.model = (const uint32_t *)(base + off_model);
+    P.model_words = (uint32_t)model->dec.words.size();
+    P.model_in_smem = in_smem;
+    P.sel = mode == MODE_PROVISO ? (uint32_t *)(base + off_sel) : nullptr;
+    P.levels = (unsigned long long *)(base + off_levels);
+    P.ctrl = d_ctrl;
+    P.seed = opts->seed;
+    P.max_states = opts->max_states;
+    P.timeout_ns = 20ull * 1000 * 1000 * 1000;
+    P.property = (uint32_t)property;
+    P.levels_per_launch = opts->kernel_iters > 0 ? (uint32_t)opts->kernel_iters : 0;
+    P.total_warps = (uint32_t)(blocks * (threads / 32));
+
+    // clear what must start at zero (the array keeps the previous call's contents)
+    cudaStream_t st = 0;
+    Ctrl c;
+    memset(&c, 0, sizeof c);
+    c.store_count = 1;
+    c.hi = 1;
+    c.nlevels = 1;
+    c.claim = 32;
+    c.phase = mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND;
+    GPX_CUDA(cudaMemcpyAsync(base + off_model, model->dec.words.data(), model_bytes, cudaMemcpyHostToDevice, st));
+    GPX_CUDA(cudaMemsetAsync(P.table, 0, tb, st));
+    GPX_CUDA(cudaMemsetAsync(d_scalar, 0, 64, st));
+    GPX_CUDA(cudaMemcpyAsync(d_ctrl, &c, sizeof c, cudaMemcpyHostToDevice, st));
+    ks.init<<<1, 32, 0, st>>>(P);
+    GPX_CUDA(cudaGetLastError());
+    GPX_CUDA(cudaStreamSynchronize(st));
+    auto t_kernels = std::chrono::steady_clock::now();
+    void *args[] = {&P};
+    unsigned long long launches = 0;
+    for (;;) {
+        GPX_CUDA(cudaLaunchCooperativeKernel((const void *)ks.explore[mode], dim3(blocks), dim3(threads), args, smem,
+                                             st));
+        launches++;
+        GPX_CUDA(cudaMemcpyAsync(&c, d_ctrl, sizeof c, cudaMemcpyDeviceToHost, st));
+        GPX_CUDA(cudaStreamSynchronize(st));
+        if (c.done || c.error) break;
+        unsigned int zero = 0;
+        GPX_CUDA(cudaMemcpyAsync(&d_ctrl->pause, &zero, sizeof zero, cudaMemcpyHostToDevice, st));
+        GPX_CUDA(cudaMemcpyAsync(&d_ctrl->launch_levels, &zero, sizeof zero, cudaMemcpyHostToDevice, st));
+    }
+    auto t_end = std::chrono::steady_clock::now();
+    unsigned long long count = std::min<unsigned long long>(c.store_count, cap);
+    int hb = (int)std::max<unsigned long long>(1, std::min<unsigned long long>((count + 255) / 256, 4096));
+    if (kind == 0)
+        set_hash_kernel<K32><<<hb, 256, 0, st>>>((const K32 *)P.store, count, model->dec.key_words, d_scalar);
+    else if (kind == 1)
+        set_hash_kernel<K64><<<hb, 256, 0, st>>>((const K64 *)P.store, count, model->dec.key_words, d_scalar);
+    else
+        set_hash_kernel<K128><<<hb, 256, 0, st>>>((const K128 *)P.store, count, model->dec.key_words, d_scalar);
+    GPX_CUDA(cudaGetLastError());
+    unsigned long long h = 0;
+    GPX_CUDA(cudaMemcpyAsync(&h, d_scalar, sizeof h, cudaMemcpyDeviceToHost, st));
+    uint32_t ncopy = std::min<uint32_t>(c.nlevels, level_capacity);
+    if (ncopy)
+        GPX_CUDA(cudaMemcpyAsync(level_counts, P.levels, sizeof(uint64_t) * ncopy, cudaMemcpyDeviceToHost, st));
+    GPX_CUDA(cudaStreamSynchronize(st));
+
+    r->status = c.error ? (int)c.error : GPX_OK;
+    r->stopped = c.error ? GPX_STOP_ERROR : (int)c.stop;
+    r->verdict = (c.stop == GPX_STOP_VIOLATION) ? property : GPX_PROP_NONE;
+    r->states = count;
+    r->nlevels = c.nlevels;
+    r->level_counts = level_counts;
+    r->transitions = c.inserts_lookups;
+    r->probes = c.probes;
+    r->inserts = c.inserts;
+    r->lookups = c.lookups;
+    r->expanded = c.expanded;
+    r->launches = launches;
+    r->kernel_ms = std::chrono::duration<double, std::milli>(t_end - t_kernels).count();
+    r->explore_ms = r->kernel_ms;
+    r->setup_ms = std::chrono::duration<double, std::milli>(t_kernels - t_start).count();
+    r->set_hash = h;
+    r->key_words = model->dec.key_words;
+    r->table_slots = P.nbuckets * ks.bucket_slots;
+    r->slot_bytes = ks.slot_bytes;
+    r->blocks = (uint32_t)blocks;
+    r->threads = (uint32_t)threads;
+    return r->status;
+}

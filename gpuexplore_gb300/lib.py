@@ -25,7 +25,7 @@ EXPORTS = [
     "gpx_status_string", "gpx_abi_version", "gpx_device_info_get", "gpx_options_init", "gpx_model_load",
     "gpx_model_load_file", "gpx_model_from_words", "gpx_model_info_get", "gpx_model_free", "gpx_explore",
     "gpx_explorer_create", "gpx_explorer_run", "gpx_explorer_set_model", "gpx_explorer_destroy",
-    "gpx_result_free", "gpx_explorer_dump",
+    "gpx_result_free", "gpx_explorer_dump", "gpx_explore_noalloc",
 ]
 
 
@@ -102,6 +102,8 @@ def load(path: str = LIB) -> C.CDLL:
     lib.gpx_result_free.argtypes = [C.POINTER(Result)]
     lib.gpx_result_free.restype = None
     lib.gpx_explorer_dump.argtypes = [vp, C.c_char_p]
+    lib.gpx_explore_noalloc.argtypes = [vp, C.POINTER(Options), C.POINTER(C.c_uint64), C.c_uint32,
+                                        C.POINTER(Result)]
     _lib = lib
     return lib
 
@@ -255,6 +257,23 @@ def explore(path_or_model, check: bool = True, **kw) -> Dict:
         lib.gpx_result_free(C.byref(r))
     if check and rc != GPX_OK:
         raise GpxError(rc, "exploring")
+    d["rc"] = rc
+    return d
+
+
+def explore_noalloc(model: Model, level_capacity: int = 1 << 16, check: bool = True, **kw) -> Dict:
+    """gpx_explore_noalloc: the exploration with all device scratch in the library's
+    static array (no allocation by the library).  The level counts land in a
+    caller-owned array; the result is not passed to gpx_result_free."""
+    lib = load()
+    o = options(**kw)
+    levels = (C.c_uint64 * max(1, level_capacity))()
+    r = Result()
+    rc = lib.gpx_explore_noalloc(model.handle, C.byref(o), levels, level_capacity, C.byref(r))
+    r.nlevels = min(r.nlevels, level_capacity)
+    d = _result_dict(r) if rc == GPX_OK or r.level_counts else {"status": rc}
+    if check and rc != GPX_OK:
+        raise GpxError(rc, "exploring without allocation")
     d["rc"] = rc
     return d
 

@@ -152,6 +152,37 @@ void gpx_explorer_destroy(gpx_explorer *ex);
 
 void gpx_result_free(gpx_result *result);
 
+/* Exploration that allocates no memory -- no counterpart in the reference.
+ *
+ * For callers that must not call cudaMalloc: code that runs while a framework's
+ * caching allocator owns the device memory (an allocation outside it can fail
+ * at the memory cap or fragment its pool), and latency-sensitive loops where
+ * cudaMalloc/cudaFree would synchronise the device.  The hash table, state
+ * store, level counts and control block live in one file-scope static device
+ * array of GPX_NOALLOC_SCRATCH_BYTES (64 MiB), which every GPU that loads the
+ * library holds until the process exits; this call uses no cudaMalloc, cudaFree
+ * or other allocating routine, on the device or the host.
+ *
+ * Sizes: opts->q_words (table, 32-bit words) and opts->store_states may be 0
+ * (split what is left of the array after the control block, 8 MiB of level
+ * counts and the model) or explicit; a request that does not fit in the array
+ * is rejected with GPX_ERR_INVALID and a message on stderr.
+ * Inputs: the model (host handle; its words are copied into the array).
+ * Outputs: `result` as gpx_explorer_run fills it, except that
+ * result->level_counts points at the caller's `level_counts` array (the first
+ * min(nlevels, level_capacity) entries are written; result->nlevels is the full
+ * count), states_buf stays NULL, no -v output is printed, and explore_ms /
+ * kernel_ms are host wall-clock times.  Do not pass this result to
+ * gpx_result_free.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before
+ * any stream capture.  Every call on a device shares the one array and leaves
+ * its contents behind (each call clears what it needs cleared), so calls whose
+ * GPU work overlaps -- from two host threads, or on two streams -- race. */
+#define GPX_NOALLOC_SCRATCH_BYTES (64u << 20)
+int gpx_explore_noalloc(const gpx_model *model, const gpx_options *opts, uint64_t *level_counts,
+                        uint32_t level_capacity, gpx_result *result);
+
 /* Write the visited set of the last run in the reference's --dump format
  * (print_local_queue, GPUexplore.cu:594-612): one state per line, local states
  * comma separated, then the stripped state-vector words. */
