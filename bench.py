@@ -43,6 +43,7 @@ BUDGET = 100_000_000
 Q_WORDS = 5_000_000_000
 CPU_SAMPLE_BUDGET = 10_000_000  # stops after BFS level 8 (about 4.2e7 states)
 WORKLOAD = "config-2 random gpf network (16 procs + monitor, seed 2024), -d, BFS to 1e8-state budget"
+KERNEL_BUILD = "converged-materialise-v2-fetch32"  # names the kernel version a committed traffic capture belongs to
 
 
 def measured_peaks():
@@ -117,6 +118,21 @@ def algorithmic_bytes(r, sv_nints):
     return 32 * r["lookups"] + 32 * r["inserts"] + 2 * 4 * sv_nints * r["expanded"]
 
 
+def max_over_ranks(step_ms, e2e_s, dist):
+    """Slowest replica's step time and end-to-end time (replicas run concurrently)."""
+    if dist is None:
+        return step_ms, e2e_s
+    import torch
+    t = torch.tensor([step_ms, e2e_s], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0]), float(t[1])
+
+
+def job_value(states_per_rank, step_ms, world):
+    """Whole-job states per second: every replica explores its own copy."""
+    return states_per_rank * world / (step_ms / 1000.0)
+
+
 def cpu_oracle_run(path, threads, budget):
     from gpuexplore_gb300.build import ORACLE
     out = subprocess.run([ORACLE, path, "-d", "--threads", str(threads), "--max-states", str(budget)],
@@ -160,6 +176,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpx", choices=["gpx", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--budget", type=int, default=BUDGET,
+                    help="state budget (smaller values give the profiling cases of the same network)")
+    ap.add_argument("--q-words", type=int, default=Q_WORDS, help="hash table size in 32-bit words")
+    ap.add_argument("--store-states", type=int, default=0, help="state store capacity (0: table slots)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -180,7 +200,8 @@ def main():
     net, words = make_network_words()
     sv_nints = (net.firstbit()[-1] + 1 + 31) // 32  # the reference's words per vector
     model = lib.Model.from_words(words)
-    opts = lib.options(property="deadlock", q_words=Q_WORDS, max_states=BUDGET, device=local)
+    opts = lib.options(property="deadlock", q_words=args.q_words, max_states=args.budget,
+                       store_states=args.store_states, device=local)
     ex = lib.Explorer(model, opts)
 
     def barrier():
@@ -213,33 +234,31 @@ def main():
     r = results[-1]
     for x in results + [r2]:
         assert x["states"] == r["states"] and x["levels"] == r["levels"] and x["set_hash"] == r["set_hash"]
-    step_ms = sum(dev_ms) / len(dev_ms)
-    e2e_step = sum(e2e_s) / len(e2e_s)
-    if dist:
-        import torch
-        t = torch.tensor([step_ms, e2e_step], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms, e2e_step = float(t[0]), float(t[1])
-    states_job = r["states"] * world
-    value = states_job / (step_ms / 1000.0)
-    e2e = states_job / e2e_step
+    step_ms, e2e_step = max_over_ranks(sum(dev_ms) / len(dev_ms), sum(e2e_s) / len(e2e_s), dist)
+    value = job_value(r["states"], step_ms, world)
+    e2e = job_value(r["states"], e2e_step * 1000.0, world)
     abytes = algorithmic_bytes(r, sv_nints)
     kms = sum(ker_ms) / len(ker_ms)
     peaks, peak_kind = measured_peaks()
     achieved = abytes / (kms / 1000.0) / 1e9
+    # DRAM traffic per launch of this workload, from the committed ncu capture
+    # (dram__bytes_read.sum + dram__bytes_write.sum, one pass, same command)
     traffic = None
     prof = os.path.join(ROOT, "profiles", "explore_kernel_config2.json")
     if os.path.exists(prof):
         with open(prof) as f:
             pj = json.load(f)
-        if pj.get("dram_bytes_per_state"):
-            traffic = pj["dram_bytes_per_state"] * r["states"]
+        if pj.get("states") == r["states"] and pj.get("kernel_build") == KERNEL_BUILD:
+            traffic = pj["dram_bytes_read"] + pj["dram_bytes_write"]
+    # the random-access ceiling: 32-byte sectors gathered at random over 20 GB
+    gathers = lib.random_gather_rate(local, 20 << 30)
     line = {
         "metric": "new states/s", "value": value, "unit": "states/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded gpf generator)",
         "config": {"workload": WORKLOAD, "states": r["states"], "levels": len(r["levels"]),
-                   "table_gb": Q_WORDS * 4 / 1e9, "slot_bytes": r["slot_bytes"], "blocks": r["blocks"],
+                   "budget": args.budget, "table_gb": args.q_words * 4 / 1e9, "slot_bytes": r["slot_bytes"],
+                   "blocks": r["blocks"],
                    "threads": r["threads"], "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (20 GB table, re-initialised every step)"},
         "e2e": {"value": e2e, "unit": "states/s", "h2d_bytes_per_step": h2d + 160,
@@ -249,7 +268,12 @@ def main():
                      "peak_source": f"{peak_kind} hbm_gbs", "kernel": "explore_kernel",
                      "kernel_ms": kms, "algorithmic_bytes": abytes,
                      "lookups": r["lookups"], "inserts": r["inserts"], "expanded": r["expanded"],
-                     "probes": r["probes"]},
+                     "probes": r["probes"],
+                     "random_access": {"probes_per_s": r["probes"] / (kms / 1000.0),
+                                       "peak_gathers_per_s": gathers,
+                                       "frac": r["probes"] / (kms / 1000.0) / gathers,
+                                       "how": "gpx_random_gather_probe: random 32 B sectors over 20 GB, "
+                                              "the probe's load instruction"}},
         "clocks": clk,
         "gpu_launches": sum(x["launches"] + 2 for x in results),
         "hash_probe_gbs": 32 * r["probes"] / (kms / 1000.0) / 1e9,

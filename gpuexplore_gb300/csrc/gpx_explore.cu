@@ -419,6 +419,19 @@ template <int MODE> __device__ void close_phase(const Params &P) {
     if (P.levels_per_launch && c->launch_levels >= P.levels_per_launch && !c->done) c->pause = 1;
 }
 
+// Spin (with back-off) until *word differs from `old`, for at most timeout_ns.
+// Returns false when the limit ran out: every device-side wait here ends.
+__device__ bool wait_change(const unsigned int *word, unsigned int old, unsigned long long timeout_ns) {
+    uint64_t t0 = globaltimer();
+    unsigned int ns = 32;
+    while (vload(word) == old) {
+        __nanosleep(ns);
+        if (ns < 1024) ns <<= 1;
+        if (globaltimer() - t0 > timeout_ns) return false;
+    }
+    return true;
+}
+
 // Grid-wide barrier; the last block to arrive closes the phase.  The wait is
 // bounded: after timeout_ns it records GPX_ERR_TIMEOUT and returns.
 template <int MODE> __device__ void grid_barrier(const Params &P) {
@@ -434,18 +447,9 @@ template <int MODE> __device__ void grid_barrier(const Params &P) {
             c->bar_count = 0;
             __threadfence();
             atomicAdd(&c->bar_gen, 1u);
-        } else {
-            uint64_t t0 = globaltimer();
-            unsigned int ns = 32;
-            while (vload(&c->bar_gen) == gen) {
-                __nanosleep(ns);
-                if (ns < 1024) ns <<= 1;
-                if (globaltimer() - t0 > P.timeout_ns) {
-                    set_error(c, GPX_ERR_TIMEOUT);
-                    atomicMax(&c->timeout_at, 1u);
-                    break;
-                }
-            }
+        } else if (!wait_change(&c->bar_gen, gen, P.timeout_ns)) {
+            set_error(c, GPX_ERR_TIMEOUT);
+            atomicMax(&c->timeout_at, 1u);
         }
         __threadfence();
     }
@@ -1244,6 +1248,19 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     void *args[] = {&P};
     unsigned long long launches = 0;
     float kernel_ms = 0;
+    // Hash probes are random 32-byte reads: ask L2 to fetch no more than a sector
+    // per miss (unset, a miss fills 128 bytes; the request rate is the same either
+    // way, the DRAM traffic is not).  The caller's limit is restored afterwards.
+    size_t saved_fetch = 0;
+    bool restore_fetch = cudaDeviceGetLimit(&saved_fetch, cudaLimitMaxL2FetchGranularity) == cudaSuccess &&
+                         cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, 32) == cudaSuccess;
+    struct FetchRestore {
+        bool on;
+        size_t v;
+        ~FetchRestore() {
+            if (on) cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, v);
+        }
+    } fetch_restore{restore_fetch, saved_fetch};
     for (;;) {
         GPX_CUDA(cudaEventRecord(ex->ev[2], ex->st));
         GPX_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(ex->blocks), dim3(ex->threads), args, ex->smem,
@@ -1388,6 +1405,99 @@ int gpx_explorer_dump(gpx_explorer *ex, const char *path) {
 }
 
 } // extern "C"
+
+// ======================================================= bounded-wait self-test
+
+namespace gpx {
+// Waits with wait_change() on a flag that nothing sets; it must give up.
+__global__ void wait_selftest_kernel(const unsigned int *flag, unsigned long long timeout_ns, unsigned int *status,
+                                     unsigned long long *waited_ns) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    uint64_t t0 = globaltimer();
+    bool changed = wait_change(flag, 0u, timeout_ns);
+    *waited_ns = globaltimer() - t0;
+    *status = changed ? GPX_OK : GPX_ERR_TIMEOUT;
+}
+} // namespace gpx
+
+extern "C" int gpx_selftest_bounded_wait(int device, uint64_t timeout_ns, uint64_t *waited_ns) {
+    if (!waited_ns || timeout_ns == 0 || timeout_ns > 10ull * 1000 * 1000 * 1000) return GPX_ERR_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPX_ERR_NO_GPU;
+    GPX_CUDA(cudaSetDevice(device));
+    unsigned int *d = nullptr;
+    GPX_CUDA(cudaMalloc(&d, 64));
+    cudaMemset(d, 0, 64);
+    wait_selftest_kernel<<<1, 32>>>(d, timeout_ns, d + 1, (unsigned long long *)(d + 2));
+    unsigned int h[4] = {0, 0, 0, 0};
+    cudaError_t e = cudaMemcpy(h, d, 16, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return GPX_ERR_CUDA;
+    *waited_ns = (uint64_t)h[2] | ((uint64_t)h[3] << 32);
+    return (int)h[1];
+}
+
+// ======================================================= random-access roofline probe
+
+namespace gpx {
+// One random 32-byte sector per thread per iteration, read with the hash
+// probe's load (ld.global.cg, 256 bits).  The XOR keeps the loads alive.
+__global__ void random_gather_kernel(const uint32_t *buf, unsigned long long nsec, int iters,
+                                     unsigned long long seed, uint32_t *sink) {
+    uint32_t acc = 0;
+    unsigned long long tid = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    for (int i = 0; i < iters; i++) {
+        unsigned long long s = __umul64hi(mix64(seed ^ (tid * 0x9E3779B97F4A7C15ull + (unsigned)i)), nsec);
+        uint32_t w[8];
+        ld256_cg(buf + 8 * s, w);
+        acc ^= w[0] ^ w[7];
+    }
+    if (acc == 0x9E3779B9u) sink[0] = acc;
+}
+} // namespace gpx
+
+extern "C" int gpx_random_gather_probe(int device, uint64_t bytes, double *gathers_per_s) {
+    if (!gathers_per_s || bytes < (1u << 20)) return GPX_ERR_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPX_ERR_NO_GPU;
+    GPX_CUDA(cudaSetDevice(device));
+    uint32_t *buf = nullptr, *sink = nullptr;
+    GPX_CUDA(cudaMalloc(&buf, bytes));
+    if (cudaMalloc(&sink, 4) != cudaSuccess) {
+        cudaFree(buf);
+        return GPX_ERR_NOMEM;
+    }
+    cudaMemset(buf, 1, bytes);
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, device);
+    const int blocks = prop.multiProcessorCount * 8, threads = 256, iters = 256;
+    // same L2 fetch hint as the explorer's runs (one sector per miss), restored below
+    size_t saved_fetch = 0;
+    bool restore = cudaDeviceGetLimit(&saved_fetch, cudaLimitMaxL2FetchGranularity) == cudaSuccess &&
+                   cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, 32) == cudaSuccess;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+        cudaEventRecord(a);
+        random_gather_kernel<<<blocks, threads>>>(buf, bytes / 32, iters, 0x5851F42D4C957F2Dull + rep, sink);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (rep > 0 && ms < best) best = ms; // the first launch warms up
+    }
+    cudaError_t e = cudaGetLastError();
+    if (restore) cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, saved_fetch);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(buf);
+    cudaFree(sink);
+    if (e != cudaSuccess) return GPX_ERR_CUDA;
+    *gathers_per_s = (double)blocks * threads * iters / (best * 1e-3);
+    return GPX_OK;
+}
 
 // ======================================================= allocation-free entry point
 //

@@ -25,7 +25,8 @@ EXPORTS = [
     "gpx_status_string", "gpx_abi_version", "gpx_device_info_get", "gpx_options_init", "gpx_model_load",
     "gpx_model_load_file", "gpx_model_from_words", "gpx_model_info_get", "gpx_model_free", "gpx_explore",
     "gpx_explorer_create", "gpx_explorer_run", "gpx_explorer_set_model", "gpx_explorer_destroy",
-    "gpx_result_free", "gpx_explorer_dump", "gpx_explore_noalloc",
+    "gpx_result_free", "gpx_explorer_dump", "gpx_explore_noalloc", "gpx_random_gather_probe",
+    "gpx_selftest_bounded_wait",
 ]
 
 
@@ -104,6 +105,8 @@ def load(path: str = LIB) -> C.CDLL:
     lib.gpx_explorer_dump.argtypes = [vp, C.c_char_p]
     lib.gpx_explore_noalloc.argtypes = [vp, C.POINTER(Options), C.POINTER(C.c_uint64), C.c_uint32,
                                         C.POINTER(Result)]
+    lib.gpx_random_gather_probe.argtypes = [i, C.c_uint64, C.POINTER(C.c_double)]
+    lib.gpx_selftest_bounded_wait.argtypes = [i, C.c_uint64, C.POINTER(C.c_uint64)]
     _lib = lib
     return lib
 
@@ -276,6 +279,23 @@ def explore_noalloc(model: Model, level_capacity: int = 1 << 16, check: bool = T
         raise GpxError(rc, "exploring without allocation")
     d["rc"] = rc
     return d
+
+
+def random_gather_rate(device: int = 0, nbytes: int = 20 << 30) -> float:
+    """Sustained random 32-byte gathers per second over an `nbytes` buffer (the
+    random-access ceiling of the hash-table probes)."""
+    v = C.c_double()
+    rc = load().gpx_random_gather_probe(device, nbytes, C.byref(v))
+    if rc != GPX_OK:
+        raise GpxError(rc, "random gather probe")
+    return v.value
+
+
+def selftest_bounded_wait(timeout_ns: int, device: int = 0):
+    """Run the device-side bounded wait on a flag nothing sets; returns (status, waited_ns)."""
+    w = C.c_uint64()
+    rc = load().gpx_selftest_bounded_wait(device, timeout_ns, C.byref(w))
+    return rc, w.value
 
 
 def device_info(device: int = 0) -> Optional[DeviceInfo]:

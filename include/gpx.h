@@ -152,6 +152,19 @@ void gpx_explorer_destroy(gpx_explorer *ex);
 
 void gpx_result_free(gpx_result *result);
 
+/* Failure-detection self-test (no reference counterpart): runs the bounded
+ * device-side wait used by the persistent kernel's grid barrier on a flag that
+ * nothing sets, with a limit of `timeout_ns` (at most 10 s).  Returns
+ * GPX_ERR_TIMEOUT with the time waited when the wait gave up as designed; the
+ * CUDA context stays usable. */
+int gpx_selftest_bounded_wait(int device, uint64_t timeout_ns, uint64_t *waited_ns);
+
+/* Random-access roofline probe (no reference counterpart; a measurement aid):
+ * gathers random 32-byte sectors from a `bytes`-sized device buffer with the
+ * same load the hash-table probes use, and reports the sustained rate in
+ * gathers per second.  Allocates and frees the buffer itself. */
+int gpx_random_gather_probe(int device, uint64_t bytes, double *gathers_per_s);
+
 /* Exploration that allocates no memory -- no counterpart in the reference.
  *
  * For callers that must not call cudaMalloc: code that runs while a framework's
