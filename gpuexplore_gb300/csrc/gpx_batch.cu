@@ -1,0 +1,608 @@
+// gpx_batch.cu -- many gpf networks explored in one persistent launch.
+//
+// Every instance keeps the single-network semantics (level-synchronous BFS,
+// verdicts, budget, cluster POR) but instances advance independently: an
+// instance's current level (or POR decide/insert phase) is an "epoch" published
+// in a 64-bit ticket (epoch << 40 | claim cursor).  Warps roam over the
+// instances, claim chunks of the published level with one atomicAdd on the
+// ticket, expand them with the same per-warp engine as the single-network
+// kernel (Explorer in gpx_device.cuh), and report the states they completed;
+// the warp that completes the last chunk of a level closes it and publishes the
+// next epoch.  No grid-wide barrier is needed, so small instances finish and
+// free the GPU for large ones.  All instances use 128-bit slots.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "gpx.h"
+#include "gpx_model.h"
+#include "gpx_device.cuh"
+
+namespace gpx {
+
+constexpr unsigned long long kCurMask = (1ull << 40) - 1;
+constexpr uint32_t kBatchLevels = 4096;
+
+struct BLevel {
+    unsigned long long lo, hi;
+    unsigned int phase, pad;
+};
+
+struct __align__(128) BInst {
+    Ctrl ctrl;                      // counters, status, stop reason, done flag, level count
+    unsigned long long ticket;      // epoch << 40 | cursor
+    BLevel lvl[2];                  // the level of each epoch parity
+    unsigned long long completed[2];
+    unsigned long long finish_ns;
+    // set up by the host
+    K128 *table;
+    unsigned long long nbuckets;
+    K128 *store;
+    unsigned long long store_cap;
+    const uint32_t *model;
+    uint32_t *sel;
+    unsigned long long *levels;
+    unsigned long long max_states;
+    uint32_t property, mode;
+};
+
+struct BGlobal {
+    unsigned int done_count;
+    unsigned int error;
+    unsigned long long start_ns;
+};
+
+struct BParams {
+    BInst *inst;
+    BGlobal *g;
+    uint32_t count;
+    uint32_t claim;
+    uint32_t max_claims;
+    uint32_t total_warps;
+    unsigned long long seed;
+    unsigned long long timeout_ns;
+};
+
+static __device__ __forceinline__ unsigned long long vload64(const unsigned long long *p) {
+    return *(volatile const unsigned long long *)p;
+}
+
+static __device__ BLevel read_level(const BInst *I, unsigned int e) {
+    const volatile BLevel *L = &I->lvl[e & 1];
+    BLevel r;
+    r.lo = L->lo;
+    r.hi = L->hi;
+    r.phase = L->phase;
+    r.pad = 0;
+    return r;
+}
+
+// Close epoch e of instance I (called by the thread that completed its last chunk).
+static __device__ void close_instance(const BParams &BP, BInst *I, unsigned int e) {
+    __threadfence();
+    BLevel L = read_level(I, e);
+    Ctrl *c = &I->ctrl;
+    BLevel next;
+    next.pad = 0;
+    if (I->mode == MODE_PROVISO && L.phase == PH_DECIDE) {
+        next.lo = L.lo;
+        next.hi = L.hi;
+        next.phase = PH_EXPAND;
+    } else {
+        unsigned long long newhi = vload(&c->store_count);
+        if (newhi > I->store_cap) newhi = I->store_cap;
+        unsigned long long cnt = newhi - L.hi;
+        if (cnt) {
+            if (c->nlevels < kBatchLevels)
+                I->levels[c->nlevels++] = cnt;
+            else
+                set_error(c, GPX_ERR_UNSUPPORTED);
+        }
+        c->level++;
+        unsigned int stop = 0xFFFFFFFFu;
+        if (vload(&c->error))
+            stop = GPX_STOP_ERROR;
+        else if (vload(&c->violation))
+            stop = GPX_STOP_VIOLATION;
+        else if (cnt == 0)
+            stop = GPX_STOP_DONE;
+        else if (I->max_states && newhi >= I->max_states)
+            stop = GPX_STOP_BUDGET;
+        if (stop != 0xFFFFFFFFu) {
+            c->stop = stop;
+            c->lo = L.hi;
+            c->hi = newhi;
+            I->finish_ns = globaltimer();
+            __threadfence();
+            c->done = 1;
+            atomicAdd(&BP.g->done_count, 1u);
+            return;
+        }
+        next.lo = L.hi;
+        next.hi = newhi;
+        next.phase = I->mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND;
+    }
+    volatile BLevel *N = &I->lvl[(e + 1) & 1];
+    N->lo = next.lo;
+    N->hi = next.hi;
+    N->phase = next.phase;
+    I->completed[(e + 1) & 1] = 0;
+    __threadfence();
+    atomicExch(&I->ticket, (unsigned long long)(e + 1) << 40);
+}
+
+template <int MODE>
+static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char *raw, unsigned long long lo,
+                                     unsigned long long off, unsigned long long cnt, bool decide) {
+    Params P;
+    memset(&P, 0, sizeof P);
+    P.table = I->table;
+    P.nbuckets = I->nbuckets;
+    P.store = I->store;
+    P.store_cap = I->store_cap;
+    P.model = I->model;
+    P.sel = I->sel;
+    P.ctrl = &I->ctrl;
+    P.seed = BP.seed;
+    P.property = I->property;
+    Explorer<K128, MODE> E(P, I->model, *(WarpScratch<K128, MODE> *)raw);
+    uint32_t B = kPairMax / E.M.n;
+    B = B > 32 ? 32 : (B < 1 ? 1 : B);
+    for (unsigned long long b = off; b < off + cnt; b += B) {
+        uint32_t n = (uint32_t)((off + cnt - b) < B ? (off + cnt - b) : B);
+        E.batch(lo + b, n, b, decide);
+    }
+    E.flush_stats(); // appends the staged new states before the chunk is reported
+}
+
+__global__ void __launch_bounds__(256, 4) batch_kernel(BParams BP) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char *raw = smem + (size_t)(threadIdx.x >> 5) * sizeof(WarpScratch<K128, MODE_PROVISO>);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t next = gwarp % BP.count;
+    uint32_t claims = 0;
+    uint64_t idle_since = 0;
+    for (;;) {
+        if (vload(&BP.g->done_count) >= BP.count || vload(&BP.g->error)) break;
+        if (BP.max_claims && claims >= BP.max_claims) break;
+        bool worked = false;
+        for (uint32_t k = 0; k < BP.count && !worked; k++) {
+            uint32_t i = next + k;
+            if (i >= BP.count) i -= BP.count;
+            BInst *I = &BP.inst[i];
+            if (vload(&I->ctrl.done)) continue;
+            unsigned long long t = vload64(&I->ticket);
+            unsigned int e = (unsigned int)(t >> 40);
+            __threadfence();
+            BLevel L = read_level(I, e);
+            unsigned long long n = L.hi - L.lo;
+            if ((t & kCurMask) >= n) continue;
+            unsigned long long claim = n / ((unsigned long long)BP.total_warps * 4ull);
+            claim = claim < BP.claim ? BP.claim : (claim > 4096 ? 4096 : claim);
+            unsigned long long old = 0;
+            if (lane == 0) old = atomicAdd(&I->ticket, claim);
+            old = __shfl_sync(kFull, old, 0);
+            unsigned int e2 = (unsigned int)(old >> 40);
+            unsigned long long cur = old & kCurMask;
+            if (e2 != e) {
+                __threadfence();
+                L = read_level(I, e2);
+                n = L.hi - L.lo;
+            }
+            if (cur >= n) continue;
+            unsigned long long cnt = (n - cur) < claim ? (n - cur) : claim;
+            bool decide = L.phase == PH_DECIDE;
+            if (I->mode == MODE_PLAIN)
+                process_claim<MODE_PLAIN>(BP, I, raw, L.lo, cur, cnt, false);
+            else if (I->mode == MODE_POR)
+                process_claim<MODE_POR>(BP, I, raw, L.lo, cur, cnt, false);
+            else
+                process_claim<MODE_PROVISO>(BP, I, raw, L.lo, cur, cnt, decide);
+            __threadfence();
+            if (lane == 0) {
+                unsigned long long d = atomicAdd(&I->completed[e2 & 1], cnt) + cnt;
+                if (d == n) close_instance(BP, I, e2);
+            }
+            __syncwarp();
+            worked = true;
+            next = i;
+            claims++;
+        }
+        if (worked) {
+            idle_since = 0;
+        } else {
+            // nothing claimable right now: other warps are finishing levels
+            __nanosleep(512);
+            uint64_t now = globaltimer();
+            if (!idle_since)
+                idle_since = now;
+            else if (now - idle_since > BP.timeout_ns) {
+                if (lane == 0) atomicCAS(&BP.g->error, 0u, (unsigned int)GPX_ERR_TIMEOUT);
+                break;
+            }
+        }
+    }
+}
+
+// Initial state of every instance (GPUexplore.cu:668-682) and the launch clock.
+__global__ void batch_init_kernel(BParams BP, int first_launch) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0 && first_launch) BP.g->start_ns = globaltimer();
+    if (i >= BP.count) return;
+    BInst *I = &BP.inst[i];
+    K128 key = KT<K128>::initial();
+    unsigned int probes = 0;
+    find_or_insert<K128>(I->table, I->nbuckets, key, KT<K128>::hash(key, BP.seed), probes);
+    I->store[0] = key;
+    I->levels[0] = 1;
+}
+
+// Per-instance order-independent set hash over each store.
+__global__ void batch_hash_kernel(const BInst *inst, uint32_t count, const uint32_t *words,
+                                  unsigned long long *out) {
+    for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
+        const BInst *I = &inst[i];
+        unsigned long long cnt = I->ctrl.store_count < I->store_cap ? I->ctrl.store_count : I->store_cap;
+        unsigned long long acc = 0;
+        for (unsigned long long j = threadIdx.x; j < cnt; j += blockDim.x) {
+            uint32_t w[4];
+            KT<K128>::words(KT<K128>::load(I->store + j), w);
+            uint64_t h = 0x9E3779B97F4A7C15ull;
+            for (uint32_t k = 0; k < words[i]; k += 2) {
+                uint64_t cc = w[k];
+                if (k + 1 < words[i]) cc |= (uint64_t)w[k + 1] << 32;
+                h = mix64(h ^ cc);
+            }
+            acc += h;
+        }
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&out[i], acc);
+    }
+}
+
+} // namespace gpx
+
+using namespace gpx;
+
+namespace {
+
+#define BCUDA(call)                                                                                           \
+    do {                                                                                                      \
+        cudaError_t _e = (call);                                                                              \
+        if (_e != cudaSuccess) {                                                                              \
+            fprintf(stderr, "gpx batch: %s failed: %s\n", #call, cudaGetErrorString(_e));                   \
+            rc = (_e == cudaErrorMemoryAllocation) ? GPX_ERR_NOMEM : GPX_ERR_CUDA;                            \
+            goto done;                                                                                        \
+        }                                                                                                     \
+    } while (0)
+
+struct BatchConfig {
+    int blocks, threads, claim, kernel_iters;
+    double load_factor;
+};
+
+struct Outcome {
+    int status, stopped, verdict;
+    uint32_t nlevels;
+    uint64_t states, set_hash, capacity;
+    double completion_ms;
+    std::vector<uint64_t> levels;
+};
+
+// Admission estimate: the state budget with a margin for the last level's
+// overshoot, bounded by the product of the local state counts.
+uint64_t estimate_capacity(const gpx_model *m, const gpx_batch_job &j) {
+    double prod = 1;
+    for (uint32_t ns : m->dec.nstates) prod *= ns;
+    double est = j.max_states ? (double)j.max_states * 8.0 : 4.0e6;
+    if (prod < est) est = prod * 1.05 + 64;
+    if (est < 1024) est = 1024;
+    return (uint64_t)est;
+}
+
+// One launch (plus -k relaunches) over `idx` instances with the given capacities.
+int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, uint64_t seed,
+               const gpx_model *const *models, const gpx_batch_job *jobs, const std::vector<uint32_t> &idx,
+               const std::vector<uint64_t> &cap, std::vector<Outcome> *out, float *device_ms, uint32_t *launches) {
+    int rc = GPX_OK;
+    const uint32_t count = (uint32_t)idx.size();
+    std::vector<BInst> h(count);
+    std::vector<uint32_t> words_per(count);
+    size_t table_bytes = 0, store_bytes = 0, sel_bytes = 0, model_words = 0;
+    std::vector<size_t> toff(count), soff(count), seloff(count), moff(count);
+    for (uint32_t k = 0; k < count; k++) {
+        const gpx_model *m = models[idx[k]];
+        uint64_t slots = (uint64_t)((double)cap[k] / cfg.load_factor) + 4;
+        uint64_t nb = (slots + 1) / 2;
+        nb = (nb + 1) & ~1ull; // even: buckets are probed in pairs
+        toff[k] = table_bytes;
+        table_bytes += nb * 32;
+        soff[k] = store_bytes;
+        store_bytes += cap[k] * sizeof(K128);
+        seloff[k] = sel_bytes;
+        if (jobs[idx[k]].por && jobs[idx[k]].cycle_proviso) sel_bytes += (cap[k] * 4 + 255) & ~(size_t)255;
+        moff[k] = model_words;
+        model_words += (m->dec.words.size() + 63) & ~(size_t)63;
+        memset(&h[k], 0, sizeof(BInst));
+        h[k].nbuckets = nb;
+        h[k].store_cap = cap[k];
+        h[k].max_states = jobs[idx[k]].max_states;
+        int prop_k = jobs[idx[k]].property;
+        if (prop_k == GPX_PROP_SAFETY && m->gpf.liveness == 1) prop_k = GPX_PROP_LIVENESS;
+        h[k].property = (uint32_t)prop_k;
+        h[k].mode = jobs[idx[k]].por ? (jobs[idx[k]].cycle_proviso ? MODE_PROVISO : MODE_POR) : MODE_PLAIN;
+        h[k].ctrl.store_count = 1;
+        h[k].ctrl.nlevels = 1;
+        h[k].ctrl.hi = 1;
+        h[k].lvl[0].lo = 0;
+        h[k].lvl[0].hi = 1;
+        h[k].lvl[0].phase = h[k].mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND;
+        words_per[k] = m->dec.key_words;
+    }
+    unsigned char *d_table = nullptr, *d_store = nullptr, *d_sel = nullptr;
+    uint32_t *d_models = nullptr, *d_words = nullptr;
+    unsigned long long *d_levels = nullptr, *d_hash = nullptr;
+    BInst *d_inst = nullptr;
+    BGlobal *d_g = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<uint32_t> hm(model_words, 0);
+    BParams BP;
+    size_t smem = 0;
+    int blocks = 0;
+    void *args[] = {&BP};
+    std::vector<unsigned long long> hh(count, 0);
+    std::vector<uint64_t> hl;
+    for (uint32_t k = 0; k < count; k++) {
+        const auto &w = models[idx[k]]->dec.words;
+        std::copy(w.begin(), w.end(), hm.begin() + moff[k]);
+    }
+    BCUDA(cudaMalloc(&d_table, std::max<size_t>(table_bytes, 256)));
+    BCUDA(cudaMalloc(&d_store, std::max<size_t>(store_bytes, 256)));
+    BCUDA(cudaMalloc(&d_sel, std::max<size_t>(sel_bytes, 256)));
+    BCUDA(cudaMalloc(&d_models, std::max<size_t>(model_words * 4, 256)));
+    BCUDA(cudaMalloc(&d_words, count * 4));
+    BCUDA(cudaMalloc(&d_levels, (size_t)count * kBatchLevels * 8));
+    BCUDA(cudaMalloc(&d_hash, count * 8));
+    BCUDA(cudaMalloc(&d_inst, count * sizeof(BInst)));
+    BCUDA(cudaMalloc(&d_g, sizeof(BGlobal)));
+    for (uint32_t k = 0; k < count; k++) {
+        h[k].table = (K128 *)(d_table + toff[k]);
+        h[k].store = (K128 *)(d_store + soff[k]);
+        h[k].sel = h[k].mode == MODE_PROVISO ? (uint32_t *)(d_sel + seloff[k]) : nullptr;
+        h[k].model = d_models + moff[k];
+        h[k].levels = d_levels + (size_t)k * kBatchLevels;
+    }
+    BCUDA(cudaMemset(d_table, 0, std::max<size_t>(table_bytes, 256)));
+    BCUDA(cudaMemset(d_hash, 0, count * 8));
+    BCUDA(cudaMemset(d_g, 0, sizeof(BGlobal)));
+    BCUDA(cudaMemcpy(d_models, hm.data(), model_words * 4, cudaMemcpyHostToDevice));
+    BCUDA(cudaMemcpy(d_words, words_per.data(), count * 4, cudaMemcpyHostToDevice));
+    BCUDA(cudaMemcpy(d_inst, h.data(), count * sizeof(BInst), cudaMemcpyHostToDevice));
+    memset(&BP, 0, sizeof BP);
+    BP.inst = d_inst;
+    BP.g = d_g;
+    BP.count = count;
+    BP.claim = (uint32_t)cfg.claim;
+    BP.max_claims = (uint32_t)std::max(0, cfg.kernel_iters);
+    BP.seed = seed;
+    BP.timeout_ns = 20ull * 1000 * 1000 * 1000;
+    smem = (size_t)(cfg.threads / 32) * sizeof(WarpScratch<K128, MODE_PROVISO>);
+    BCUDA(cudaFuncSetAttribute((const void *)batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    {
+        int per_sm = 0;
+        BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)batch_kernel, cfg.threads, smem));
+        blocks = cfg.blocks > 0 ? cfg.blocks : std::max(1, per_sm) * prop.multiProcessorCount;
+    }
+    BP.total_warps = (uint32_t)(blocks * (cfg.threads / 32));
+    BCUDA(cudaEventCreate(&ev0));
+    BCUDA(cudaEventCreate(&ev1));
+    BCUDA(cudaEventRecord(ev0));
+    batch_init_kernel<<<(count + 127) / 128, 128>>>(BP, 1);
+    BCUDA(cudaGetLastError());
+    for (;;) {
+        BCUDA(cudaLaunchKernel((const void *)batch_kernel, dim3(blocks), dim3(cfg.threads), args, smem, 0));
+        (*launches)++;
+        BGlobal g;
+        BCUDA(cudaMemcpy(&g, d_g, sizeof g, cudaMemcpyDeviceToHost));
+        if (g.done_count >= count || g.error) {
+            if (g.error) rc = (int)g.error;
+            break;
+        }
+    }
+    BCUDA(cudaEventRecord(ev1));
+    BCUDA(cudaEventSynchronize(ev1));
+    {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev0, ev1);
+        *device_ms += ms;
+    }
+    batch_hash_kernel<<<std::min<uint32_t>(count, 4096), 256>>>(d_inst, count, d_words, d_hash);
+    BCUDA(cudaGetLastError());
+    BCUDA(cudaMemcpy(h.data(), d_inst, count * sizeof(BInst), cudaMemcpyDeviceToHost));
+    BCUDA(cudaMemcpy(hh.data(), d_hash, count * 8, cudaMemcpyDeviceToHost));
+    hl.resize((size_t)count * kBatchLevels);
+    BCUDA(cudaMemcpy(hl.data(), d_levels, hl.size() * 8, cudaMemcpyDeviceToHost));
+    {
+        BGlobal g;
+        BCUDA(cudaMemcpy(&g, d_g, sizeof g, cudaMemcpyDeviceToHost));
+        out->resize(count);
+        for (uint32_t k = 0; k < count; k++) {
+            Outcome &o = (*out)[k];
+            const Ctrl &c = h[k].ctrl;
+            o.status = c.error ? (int)c.error : (c.done ? GPX_OK : (rc ? rc : GPX_ERR_TIMEOUT));
+            o.stopped = c.error ? GPX_STOP_ERROR : (int)c.stop;
+            o.verdict = (c.done && c.stop == GPX_STOP_VIOLATION) ? (int)h[k].property : GPX_PROP_NONE;
+            o.states = std::min<unsigned long long>(c.store_count, h[k].store_cap);
+            o.nlevels = c.nlevels;
+            o.set_hash = hh[k];
+            o.capacity = cap[k];
+            o.completion_ms = h[k].finish_ns > g.start_ns ? (h[k].finish_ns - g.start_ns) * 1e-6 : 0.0;
+            o.levels.assign(hl.begin() + (size_t)k * kBatchLevels,
+                            hl.begin() + (size_t)k * kBatchLevels + std::min<uint32_t>(c.nlevels, kBatchLevels));
+        }
+    }
+done:
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    cudaFree(d_table);
+    cudaFree(d_store);
+    cudaFree(d_sel);
+    cudaFree(d_models);
+    cudaFree(d_words);
+    cudaFree(d_levels);
+    cudaFree(d_hash);
+    cudaFree(d_inst);
+    cudaFree(d_g);
+    return rc;
+}
+
+double percentile(std::vector<double> v, double q) {
+    if (v.empty()) return 0;
+    std::sort(v.begin(), v.end());
+    size_t i = (size_t)std::min<double>(v.size() - 1, std::max(0.0, q * (v.size() - 1) + 0.5));
+    return v[i];
+}
+
+} // namespace
+
+extern "C" {
+
+void gpx_batch_options_init(gpx_batch_options *o) {
+    memset(o, 0, sizeof *o);
+    o->struct_size = sizeof *o;
+    o->seed = 0x243F6A8885A308D3ull;
+}
+
+void gpx_batch_job_init(gpx_batch_job *j) {
+    memset(j, 0, sizeof *j);
+    j->struct_size = sizeof *j;
+}
+
+int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs, uint32_t count,
+                      const gpx_batch_options *opts, gpx_batch_item *items, uint64_t *level_counts,
+                      uint32_t level_capacity, gpx_batch_stats *stats) {
+    if (!models || !jobs || !items || !opts || !count || opts->struct_size != sizeof(gpx_batch_options))
+        return GPX_ERR_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPX_ERR_NO_GPU;
+    if (opts->device < 0 || opts->device >= ndev) return GPX_ERR_INVALID;
+    if (cudaSetDevice(opts->device) != cudaSuccess) return GPX_ERR_CUDA;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, opts->device) != cudaSuccess) return GPX_ERR_CUDA;
+    BatchConfig cfg;
+    cfg.blocks = opts->blocks;
+    cfg.threads = opts->threads > 0 ? opts->threads : 256;
+    cfg.claim = opts->claim > 0 ? opts->claim : 64;
+    cfg.kernel_iters = opts->kernel_iters;
+    cfg.load_factor = opts->load_factor > 0 ? opts->load_factor : 0.5;
+    if (cfg.threads % 32 || cfg.threads > 256 || cfg.load_factor > 0.95) return GPX_ERR_INVALID;
+    const int max_adm = opts->max_admissions > 0 ? opts->max_admissions : 3;
+    gpx_batch_stats st;
+    memset(&st, 0, sizeof st);
+
+    std::vector<uint32_t> todo;
+    std::vector<uint64_t> cap(count, 0);
+    for (uint32_t i = 0; i < count; i++) {
+        memset(&items[i], 0, sizeof items[i]);
+        if (!models[i] || jobs[i].struct_size != sizeof(gpx_batch_job)) return GPX_ERR_INVALID;
+        if (models[i]->dec.state_bits > (uint32_t)kMaxStateBits) {
+            items[i].status = GPX_ERR_UNSUPPORTED;
+            items[i].stopped = GPX_STOP_ERROR;
+            continue;
+        }
+        cap[i] = jobs[i].capacity ? jobs[i].capacity : estimate_capacity(models[i], jobs[i]);
+        todo.push_back(i);
+    }
+    // the request rate of random hash probes bounds these kernels: fetch one sector per L2 miss
+    size_t saved_fetch = 0;
+    bool restore = cudaDeviceGetLimit(&saved_fetch, cudaLimitMaxL2FetchGranularity) == cudaSuccess &&
+                   cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, 32) == cudaSuccess;
+
+    if (opts->autotune && todo.size() > 1) {
+        // tune on an evenly spaced sample of at most 48 instances
+        auto t0 = std::chrono::steady_clock::now();
+        std::vector<uint32_t> sample;
+        size_t step = std::max<size_t>(1, todo.size() / 48);
+        for (size_t k = 0; k < todo.size() && sample.size() < 48; k += step) sample.push_back(todo[k]);
+        std::vector<uint64_t> scap;
+        for (uint32_t i : sample) scap.push_back(cap[i]);
+        double best = 1e30;
+        BatchConfig bestc = cfg;
+        for (int threads : {128, 256})
+            for (int claim : {32, 64, 128, 256})
+                for (double lf : {0.25, 0.5}) {
+                    BatchConfig c = cfg;
+                    c.threads = threads;
+                    c.claim = claim;
+                    c.load_factor = lf;
+                    std::vector<Outcome> o;
+                    float ms = 0;
+                    uint32_t l = 0;
+                    if (run_launch(opts->device, prop, c, opts->seed, models, jobs, sample, scap, &o, &ms, &l) ==
+                            GPX_OK &&
+                        ms < best) {
+                        best = ms;
+                        bestc = c;
+                    }
+                }
+        cfg = bestc;
+        st.tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+
+    int rc = GPX_OK;
+    std::vector<double> completion;
+    for (int adm = 1; adm <= max_adm && !todo.empty(); adm++) {
+        std::vector<uint64_t> c2;
+        for (uint32_t i : todo) c2.push_back(cap[i]);
+        std::vector<Outcome> out;
+        float ms = 0;
+        rc = run_launch(opts->device, prop, cfg, opts->seed, models, jobs, todo, c2, &out, &ms, &st.launches);
+        st.device_ms += ms;
+        if (rc != GPX_OK && out.empty()) break;
+        std::vector<uint32_t> again;
+        for (size_t k = 0; k < todo.size(); k++) {
+            uint32_t i = todo[k];
+            const Outcome &o = out[k];
+            gpx_batch_item &it = items[i];
+            it.admissions = (uint32_t)adm;
+            it.status = o.status;
+            it.stopped = o.stopped;
+            it.verdict = o.verdict;
+            it.states = o.states;
+            it.nlevels = o.nlevels;
+            it.set_hash = o.set_hash;
+            it.capacity = o.capacity;
+            it.completion_ms = o.completion_ms;
+            if (adm == 1 && o.status == GPX_OK) completion.push_back(o.completion_ms);
+            if (level_counts && level_capacity)
+                for (uint32_t l = 0; l < std::min<uint32_t>(level_capacity, (uint32_t)o.levels.size()); l++)
+                    level_counts[(size_t)i * level_capacity + l] = o.levels[l];
+            if ((o.status == GPX_ERR_TABLE_FULL || o.status == GPX_ERR_STORE_FULL) && adm < max_adm) {
+                cap[i] *= 4; // re-admit with a bigger partition
+                again.push_back(i);
+            }
+        }
+        todo.swap(again);
+        if (rc != GPX_OK && rc != GPX_ERR_TABLE_FULL && rc != GPX_ERR_STORE_FULL) break;
+        rc = GPX_OK;
+    }
+    if (restore) cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, saved_fetch);
+    for (uint32_t i = 0; i < count; i++) st.states += items[i].states;
+    st.p50_ms = percentile(completion, 0.50);
+    st.p99_ms = percentile(completion, 0.99);
+    st.claim = cfg.claim;
+    st.threads = cfg.threads;
+    st.blocks = cfg.blocks;
+    st.load_factor = cfg.load_factor;
+    if (stats) *stats = st;
+    return rc;
+}
+
+} // extern "C"

@@ -49,332 +49,9 @@
 #include "gpx.h"
 #include "gpx_model.h"
 
-struct gpx_model {
-    gpx::Gpf gpf;
-    gpx::Decoded dec;
-};
+#include "gpx_device.cuh"
 
 namespace gpx {
-
-// ------------------------------------------------------------------ constants
-
-constexpr uint32_t kFull = 0xFFFFFFFFu;
-constexpr int kPairMax = 256;   // (state, process) pairs staged per warp batch
-constexpr int kMaxProbe = 32;   // buckets probed before reporting the table full
-constexpr uint32_t kMaxLevels = 1u << 20;
-
-enum Mode : int { MODE_PLAIN = 0, MODE_POR = 1, MODE_PROVISO = 2 };
-enum Phase : uint32_t { PH_EXPAND = 0, PH_DECIDE = 1 };
-
-// Control block shared by all blocks of the persistent kernel.
-struct Ctrl {
-    unsigned long long store_count; // states appended to the store
-    unsigned long long lo, hi;      // the level being expanded: store indices [lo, hi)
-    unsigned long long cursor;      // next unclaimed offset within [lo, hi)
-    unsigned long long lookups, probes, expanded, inserts, inserts_lookups;
-    unsigned int claim;             // states per claim
-    unsigned int level;             // BFS depth of [lo, hi)
-    unsigned int nlevels;           // recorded level counts
-    unsigned int done;              // exploration finished
-    unsigned int pause;             // launch budget (-k) reached: kernel returns, host relaunches
-    unsigned int violation;         // property violated during this level
-    unsigned int error;             // gpx_status
-    unsigned int stop;              // gpx_stop
-    unsigned int phase;             // Phase
-    unsigned int launch_levels;     // levels closed in this launch
-    unsigned int bar_count, bar_gen;
-    unsigned int timeout_at;        // where a bounded wait gave up (diagnostics)
-};
-
-struct Params {
-    void *table;
-    unsigned long long nbuckets;
-    void *store;
-    unsigned long long store_cap;
-    const uint32_t *model; // device layout (gpx_model.h)
-    uint32_t model_words;
-    uint32_t model_in_smem;
-    uint32_t *sel;         // per-frontier-state cluster (cycle proviso)
-    unsigned long long *levels;
-    Ctrl *ctrl;
-    unsigned long long seed;
-    unsigned long long max_states;
-    unsigned long long timeout_ns;
-    uint32_t property;
-    uint32_t levels_per_launch;
-    uint32_t total_warps;
-};
-
-// ------------------------------------------------------------- device helpers
-
-__device__ __forceinline__ uint64_t mix64(uint64_t z) { // SplitMix64 finaliser (Steele, Lea, Flood 2014)
-    z += 0x9E3779B97F4A7C15ull;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-
-__device__ __forceinline__ uint64_t globaltimer() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ void ld256_cg(const void *p, uint32_t (&w)[8]) {
-    asm volatile("ld.global.cg.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
-                 : "l"(p));
-}
-
-__device__ __forceinline__ uint64_t lmask(uint32_t w) { return (w >= 64) ? ~0ull : ((1ull << w) - 1ull); }
-
-// Keys are stored in slot form: the packed state vector plus an occupancy
-// marker in the top bit of each 32/64-bit half, so an all-zero slot is empty
-// and the all-zero state vector is a valid key.
-struct K32 { uint32_t v; };
-struct K64 { unsigned long long v; };
-struct __align__(16) K128 { unsigned long long lo, hi; };
-
-template <class K> struct KT;
-
-template <> struct KT<K32> {
-    static constexpr int kSlots = 8; // 32-byte bucket
-    __device__ static K32 initial() { return {0x80000000u}; }
-    __device__ static bool eq(const K32 &a, const K32 &b) { return a.v == b.v; }
-    __device__ static bool empty(const K32 &a) { return a.v == 0; }
-    __device__ static bool torn(const K32 &) { return false; }
-    __device__ static uint32_t get(const K32 &k, uint32_t f, uint32_t w) { return (k.v >> f) & (uint32_t)lmask(w); }
-    __device__ static void set(K32 &k, uint32_t f, uint32_t w, uint32_t x) {
-        uint32_t m = (uint32_t)lmask(w) << f;
-        k.v = (k.v & ~m) | ((x << f) & m);
-    }
-    __device__ static uint64_t hash(const K32 &k, uint64_t seed) { return mix64((uint64_t)k.v ^ seed); }
-    __device__ static K32 cas(K32 *p, K32 cmp, K32 val) { return {atomicCAS(&p->v, cmp.v, val.v)}; }
-    __device__ static void bucket(const K32 *b, K32 (&s)[kSlots]) {
-        uint32_t w[8];
-        ld256_cg(b, w);
-#pragma unroll
-        for (int j = 0; j < 8; j++) s[j].v = w[j];
-    }
-    __device__ static K32 load(const K32 *p) { return {__ldcg(&p->v)}; }
-    __device__ static void words(const K32 &k, uint32_t (&w)[4]) {
-        w[0] = k.v & 0x7FFFFFFFu;
-        w[1] = w[2] = w[3] = 0;
-    }
-};
-
-template <> struct KT<K64> {
-    static constexpr int kSlots = 4; // 32-byte bucket
-    __device__ static K64 initial() { return {0x8000000000000000ull}; }
-    __device__ static bool eq(const K64 &a, const K64 &b) { return a.v == b.v; }
-    __device__ static bool empty(const K64 &a) { return a.v == 0; }
-    __device__ static bool torn(const K64 &) { return false; }
-    __device__ static uint32_t get(const K64 &k, uint32_t f, uint32_t w) { return (uint32_t)((k.v >> f) & lmask(w)); }
-    __device__ static void set(K64 &k, uint32_t f, uint32_t w, uint32_t x) {
-        unsigned long long m = lmask(w) << f;
-        k.v = (k.v & ~m) | (((unsigned long long)x << f) & m);
-    }
-    __device__ static uint64_t hash(const K64 &k, uint64_t seed) { return mix64(k.v ^ seed); }
-    __device__ static K64 cas(K64 *p, K64 cmp, K64 val) { return {atomicCAS(&p->v, cmp.v, val.v)}; }
-    __device__ static void bucket(const K64 *b, K64 (&s)[kSlots]) {
-        uint32_t w[8];
-        ld256_cg(b, w);
-#pragma unroll
-        for (int j = 0; j < 4; j++) s[j].v = (unsigned long long)w[2 * j] | ((unsigned long long)w[2 * j + 1] << 32);
-    }
-    __device__ static K64 load(const K64 *p) { return {__ldcg(&p->v)}; }
-    __device__ static void words(const K64 &k, uint32_t (&w)[4]) {
-        unsigned long long v = k.v & 0x7FFFFFFFFFFFFFFFull;
-        w[0] = (uint32_t)v;
-        w[1] = (uint32_t)(v >> 32);
-        w[2] = w[3] = 0;
-    }
-};
-
-// 128-bit slots hold 63 state bits in each 64-bit half (bit 63 of both halves
-// is the occupancy marker).  Each half is read atomically, so a slot caught in
-// the middle of its insertion shows exactly one zero half ("torn"); such a slot
-// is re-read with an atomic before it is judged.
-template <> struct KT<K128> {
-    static constexpr int kSlots = 2; // 32-byte bucket
-    static constexpr unsigned long long kOcc = 0x8000000000000000ull;
-    __device__ static K128 initial() { return {kOcc, kOcc}; }
-    __device__ static bool eq(const K128 &a, const K128 &b) { return a.lo == b.lo && a.hi == b.hi; }
-    __device__ static bool empty(const K128 &a) { return (a.lo | a.hi) == 0; }
-    __device__ static bool torn(const K128 &a) { return (a.lo == 0) != (a.hi == 0); }
-    __device__ static uint32_t get(const K128 &k, uint32_t f, uint32_t w) {
-        if (f + w <= 63) return (uint32_t)((k.lo >> f) & lmask(w));
-        if (f >= 63) return (uint32_t)((k.hi >> (f - 63)) & lmask(w));
-        uint32_t nlo = 63 - f;
-        return (uint32_t)(((k.lo >> f) & lmask(nlo)) | ((k.hi & lmask(w - nlo)) << nlo));
-    }
-    __device__ static void set(K128 &k, uint32_t f, uint32_t w, uint32_t x) {
-        if (f + w <= 63) {
-            unsigned long long m = lmask(w) << f;
-            k.lo = (k.lo & ~m) | (((unsigned long long)x << f) & m);
-        } else if (f >= 63) {
-            unsigned long long m = lmask(w) << (f - 63);
-            k.hi = (k.hi & ~m) | (((unsigned long long)x << (f - 63)) & m);
-        } else {
-            uint32_t nlo = 63 - f;
-            unsigned long long ml = lmask(nlo) << f, mh = lmask(w - nlo);
-            k.lo = (k.lo & ~ml) | (((unsigned long long)x << f) & ml);
-            k.hi = (k.hi & ~mh) | (((unsigned long long)x >> nlo) & mh);
-        }
-    }
-    __device__ static uint64_t hash(const K128 &k, uint64_t seed) { return mix64(k.lo ^ mix64(k.hi ^ seed)); }
-    __device__ static K128 cas(K128 *p, K128 cmp, K128 val) {
-        unsigned long long olo, ohi;
-        asm volatile(
-            "{\n\t.reg .b128 c, v, o;\n\t"
-            "mov.b128 c, {%2, %3};\n\t"
-            "mov.b128 v, {%4, %5};\n\t"
-            "atom.global.cas.b128 o, [%6], c, v;\n\t"
-            "mov.b128 {%0, %1}, o;\n\t}"
-            : "=l"(olo), "=l"(ohi)
-            : "l"(cmp.lo), "l"(cmp.hi), "l"(val.lo), "l"(val.hi), "l"(p)
-            : "memory");
-        return {olo, ohi};
-    }
-    __device__ static void bucket(const K128 *b, K128 (&s)[kSlots]) {
-        uint32_t w[8];
-        ld256_cg(b, w);
-        s[0].lo = (unsigned long long)w[0] | ((unsigned long long)w[1] << 32);
-        s[0].hi = (unsigned long long)w[2] | ((unsigned long long)w[3] << 32);
-        s[1].lo = (unsigned long long)w[4] | ((unsigned long long)w[5] << 32);
-        s[1].hi = (unsigned long long)w[6] | ((unsigned long long)w[7] << 32);
-    }
-    __device__ static K128 load(const K128 *p) {
-        return {__ldcg(&p->lo), __ldcg(&p->hi)};
-    }
-    __device__ static void words(const K128 &k, uint32_t (&w)[4]) {
-        unsigned long long lo = k.lo & ~kOcc, hi = k.hi & ~kOcc;
-        w[0] = (uint32_t)lo;
-        w[1] = (uint32_t)(lo >> 32) | (uint32_t)((hi & 1ull) << 31);
-        w[2] = (uint32_t)(hi >> 1);
-        w[3] = (uint32_t)(hi >> 33);
-    }
-};
-
-// Probe sequence of a key: 32-byte buckets visited in pairs -- a bucket, then
-// its neighbour in the same 64-byte line -- for kMaxProbe/2 hash functions.
-// The table holds an even number of buckets.
-__device__ __forceinline__ unsigned long long bucket_of(uint64_t h, int i, unsigned long long nb) {
-    int j = i >> 1;
-    uint64_t x = j ? mix64(h + (uint64_t)j * 0x9E3779B97F4A7C15ull) : h;
-    unsigned long long b = __umul64hi(x, nb);
-    return (i & 1) ? (b ^ 1ull) : b;
-}
-
-// Find-or-insert.  Returns 0 if the key was present, 1 if this call inserted
-// it, 2 if every probed bucket was full.  Slots go from empty to a key exactly
-// once; every caller scans the same probe sequence and claims the first empty
-// slot it sees with a full-key CAS, so two insertions of one key always meet in
-// the same slot and exactly one wins.
-template <class K>
-__device__ __forceinline__ int find_or_insert(K *table, unsigned long long nb, const K &key, uint64_t h,
-                                              unsigned int &probes) {
-    constexpr int S = KT<K>::kSlots;
-    for (int i = 0; i < kMaxProbe; i++) {
-        K *b = table + bucket_of(h, i, nb) * S;
-        K s[S];
-        KT<K>::bucket(b, s);
-        probes++;
-#pragma unroll
-        for (int j = 0; j < S; j++)
-            if (KT<K>::eq(s[j], key)) return 0;
-#pragma unroll
-        for (int j = 0; j < S; j++) {
-            if (KT<K>::empty(s[j]) || KT<K>::torn(s[j])) {
-                K zero;
-                memset(&zero, 0, sizeof zero);
-                K old = KT<K>::cas(b + j, zero, key);
-                if (KT<K>::empty(old)) return 1;
-                if (KT<K>::eq(old, key)) return 0;
-            }
-        }
-    }
-    return 2;
-}
-
-// Lookup in a table no one writes to during the call (the decide pass of the
-// cycle proviso): an empty slot on the probe path means the key is absent.
-template <class K>
-__device__ __forceinline__ bool find_key(K *table, unsigned long long nb, const K &key, uint64_t h,
-                                         unsigned int &probes) {
-    constexpr int S = KT<K>::kSlots;
-    for (int i = 0; i < kMaxProbe; i++) {
-        K *b = table + bucket_of(h, i, nb) * S;
-        K s[S];
-        KT<K>::bucket(b, s);
-        probes++;
-#pragma unroll
-        for (int j = 0; j < S; j++) {
-            K v = s[j];
-            if (KT<K>::torn(v)) {
-                K zero;
-                memset(&zero, 0, sizeof zero);
-                v = KT<K>::cas(b + j, zero, zero); // atomic re-read; writes nothing new
-            }
-            if (KT<K>::eq(v, key)) return true;
-            if (KT<K>::empty(v)) return false;
-        }
-    }
-    return false;
-}
-
-// --------------------------------------------------------- per-warp scratch
-
-constexpr int kStage = 64; // new states staged per warp before one store append
-
-template <class K, int MODE> struct WarpScratch {
-    static constexpr int kPor = (MODE == MODE_PLAIN) ? 1 : kPairMax;
-    K keys[32];                  // the batch's source states
-    K stage[kStage];             // new states waiting to be appended to the store
-    uint32_t appl[kPairMax];     // per pair: applicable rules among those it leads (bit r)
-    uint32_t pre[kPairMax + 1];  // per pair: successor count, then its exclusive prefix sum
-    uint32_t en[32];             // per state: some transition enabled
-    uint32_t cl0[kPor];          // per pair: static POR cluster
-    uint32_t clo[kPor];          // per pair: cluster closure
-    uint32_t prov[32], sel[32], best[32];
-};
-
-struct WarpStats {
-    unsigned int lookups, probes, inserts, expanded, ilookups;
-    unsigned int violation;
-};
-
-// Model accessors over the device layout (gpx_model.h).
-struct MView {
-    const uint32_t *w;
-    uint32_t n;
-    __device__ uint32_t fb(uint32_t p) const { return w[H_FB + p]; }
-    __device__ uint32_t bs(uint32_t p) const { return w[H_BS + p]; }
-    __device__ const uint32_t *rec(uint32_t p, uint32_t s) const {
-        return w + w[H_OFF_RECS] + (w[H_PSBASE + p] + s) * kRecWords;
-    }
-    __device__ uint32_t ltgt(uint32_t i) const { return w[w[H_OFF_LTGT] + i]; }
-    __device__ uint32_t stgt(uint32_t i) const { return w[w[H_OFF_STGT] + i]; }
-    __device__ uint32_t lrule(uint32_t i) const { return w[w[H_OFF_LRULE] + i]; }
-    __device__ uint32_t rmask(uint32_t k) const { return w[w[H_OFF_RULES] + 2 * k]; }
-    __device__ uint32_t ract(uint32_t k) const { return w[w[H_OFF_RULES] + 2 * k + 1]; }
-    // synchronising group of (p, s) for action a: {action, toff, tcnt, has1} or null
-    __device__ const uint32_t *group(const uint32_t *rec, uint32_t a) const {
-        const uint32_t *g = w + w[H_OFF_SENT] + rec[R_SOFF] * 4;
-        for (uint32_t i = 0; i < rec[R_SCNT]; i++, g += 4) {
-            if (g[0] == a) return g;
-            if (g[0] > a) break;
-        }
-        return nullptr;
-    }
-};
-
-__device__ __forceinline__ void set_error(Ctrl *c, unsigned int code) { atomicCAS(&c->error, 0u, code); }
-
-__device__ __forceinline__ unsigned int vload(const unsigned int *p) { return *(volatile const unsigned int *)p; }
-__device__ __forceinline__ unsigned long long vload(const unsigned long long *p) {
-    return *(volatile const unsigned long long *)p;
-}
 
 // Close the phase that every block has just finished (run by the last block to
 // arrive at the barrier, with all other blocks waiting).
@@ -419,19 +96,6 @@ template <int MODE> __device__ void close_phase(const Params &P) {
     if (P.levels_per_launch && c->launch_levels >= P.levels_per_launch && !c->done) c->pause = 1;
 }
 
-// Spin (with back-off) until *word differs from `old`, for at most timeout_ns.
-// Returns false when the limit ran out: every device-side wait here ends.
-__device__ bool wait_change(const unsigned int *word, unsigned int old, unsigned long long timeout_ns) {
-    uint64_t t0 = globaltimer();
-    unsigned int ns = 32;
-    while (vload(word) == old) {
-        __nanosleep(ns);
-        if (ns < 1024) ns <<= 1;
-        if (globaltimer() - t0 > timeout_ns) return false;
-    }
-    return true;
-}
-
 // Grid-wide barrier; the last block to arrive closes the phase.  The wait is
 // bounded: after timeout_ns it records GPX_ERR_TIMEOUT and returns.
 template <int MODE> __device__ void grid_barrier(const Params &P) {
@@ -455,305 +119,6 @@ template <int MODE> __device__ void grid_barrier(const Params &P) {
     }
     __syncthreads();
 }
-
-// ------------------------------------------------------------- the kernel
-
-template <class K, int MODE> struct Explorer {
-    const Params &P;
-    MView M;
-    WarpScratch<K, MODE> &ws;
-    K *table;
-    K *store;
-    uint32_t lane;
-    uint32_t lanemask_lt;
-    uint32_t shead, scount; // staged new states (warp-uniform)
-    WarpStats st;
-    bool safety, deadlock;
-
-    __device__ Explorer(const Params &p, const uint32_t *model, WarpScratch<K, MODE> &w)
-        : P(p), ws(w), table((K *)p.table), store((K *)p.store) {
-        M.w = model;
-        M.n = model[H_NPROCS];
-        lane = threadIdx.x & 31;
-        lanemask_lt = (1u << lane) - 1u;
-        shead = scount = 0;
-        st = WarpStats{0, 0, 0, 0, 0, 0};
-        safety = P.property == GPX_PROP_SAFETY;
-        deadlock = P.property == GPX_PROP_DEADLOCK;
-    }
-
-    // Successors of rule k from `key`: the product of the participants' targets.
-    __device__ uint32_t product_size(const K &key, uint32_t mask, uint32_t act) const {
-        uint32_t psz = 1, rest = mask;
-        while (rest) {
-            uint32_t q = __ffs(rest) - 1;
-            rest &= rest - 1;
-            psz *= M.group(M.rec(q, KT<K>::get(key, M.fb(q), M.bs(q))), act)[2];
-        }
-        return psz;
-    }
-
-    // Append `cnt` (<= 32) staged new states to the store with one atomic.
-    __device__ void stage_flush(uint32_t cnt) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&P.ctrl->store_count, (unsigned long long)cnt);
-        base = __shfl_sync(kFull, base, 0);
-        if (lane < cnt) {
-            unsigned long long idx = base + lane;
-            if (idx < P.store_cap)
-                store[idx] = ws.stage[(shead + lane) % kStage];
-            else
-                set_error(P.ctrl, GPX_ERR_STORE_FULL);
-        }
-        shead = (shead + cnt) % kStage;
-        scount -= cnt;
-        __syncwarp();
-    }
-
-    // Expand a batch of B states store[first .. first+B).
-    __device__ void batch(unsigned long long first, uint32_t B, unsigned long long lvl_off, bool decide) {
-        const uint32_t n = M.n;
-        if (lane < B) {
-            ws.keys[lane] = KT<K>::load(store + first + lane);
-            ws.en[lane] = 0;
-            ws.prov[lane] = 0;
-            ws.best[lane] = kFull;
-            ws.sel[lane] = kFull;
-        }
-        __syncwarp();
-        const uint32_t npairs = B * n;
-        const bool check = (MODE != MODE_PROVISO) || decide;
-        const bool filter = (MODE == MODE_POR) || (MODE == MODE_PROVISO && !decide);
-
-        // A: enabledness, applicable rules, successor counts, static clusters,
-        //    safety on moves into monitor state 1 (GPUexplore.cu:927-935, 1063-1069)
-        for (uint32_t i = lane; i < npairs; i += 32) {
-            uint32_t g = i / n, p = i - g * n;
-            K key = ws.keys[g];
-            uint32_t s = KT<K>::get(key, M.fb(p), M.bs(p));
-            const uint32_t *rec = M.rec(p, s);
-            uint32_t lcnt = rec[R_LCNT], roff = rec[R_ROFF], rcnt = rec[R_RCNT];
-            uint32_t appl = 0, provbits = lcnt ? (1u << p) : 0u, cnt = lcnt;
-            bool viol = safety && check && p == n - 1 && (rec[R_FLAGS] & 1u);
-            for (uint32_t r = 0; r < rcnt; r++) {
-                uint32_t k = M.lrule(roff + r);
-                uint32_t mask = M.rmask(k), act = M.ract(k);
-                bool ok = true, hit1 = false;
-                uint32_t rest = mask, psz = 1;
-                while (rest) {
-                    uint32_t q = __ffs(rest) - 1;
-                    rest &= rest - 1;
-                    uint32_t sq = (q == p) ? s : KT<K>::get(key, M.fb(q), M.bs(q));
-                    const uint32_t *grp = M.group(q == p ? rec : M.rec(q, sq), act);
-                    if (!grp) {
-                        ok = false;
-                        break;
-                    }
-                    psz *= grp[2];
-                    if (q == n - 1 && grp[3]) hit1 = true;
-                }
-                if (ok) {
-                    appl |= 1u << r;
-                    provbits |= mask;
-                    cnt += psz;
-                    if (safety && check && hit1) viol = true;
-                }
-            }
-            ws.appl[i] = appl;
-            ws.pre[i] = cnt;
-            if (MODE != MODE_PLAIN) ws.cl0[i] = rec[R_CL0];
-            if (lcnt | appl) ws.en[g] = 1;
-            if (MODE == MODE_POR) atomicOr(&ws.prov[g], provbits);
-            if (viol) st.violation = 1;
-        }
-        __syncwarp();
-        if (deadlock && check && lane < B && ws.en[lane] == 0) st.violation = 1;
-        if (check && lane < B) st.expanded++;
-
-        // B: the cluster each state expands (POR); without the cycle proviso the
-        //    proviso bits are plain enabledness (GPUexplore.cu:1395-1397)
-        if (MODE == MODE_POR) select_clusters(B);
-        if (MODE == MODE_PROVISO && !decide) {
-            if (lane < B) ws.sel[lane] = __ldcg(P.sel + lvl_off + lane);
-            __syncwarp();
-        }
-        if (filter) {
-            // successors of transitions inside the cluster only (GPUexplore.cu:1409, 1541)
-            for (uint32_t i = lane; i < npairs; i += 32) {
-                uint32_t g = i / n, p = i - g * n;
-                uint32_t sel = ws.sel[g];
-                K key = ws.keys[g];
-                const uint32_t *rec = M.rec(p, KT<K>::get(key, M.fb(p), M.bs(p)));
-                uint32_t cnt = (sel >> p & 1u) ? rec[R_LCNT] : 0u;
-                uint32_t a = ws.appl[i], keep = 0, roff = rec[R_ROFF];
-                while (a) {
-                    uint32_t r = __ffs(a) - 1;
-                    a &= a - 1;
-                    uint32_t k = M.lrule(roff + r), mask = M.rmask(k);
-                    if ((mask & sel) != mask) continue;
-                    keep |= 1u << r;
-                    cnt += product_size(key, mask, M.ract(k));
-                }
-                ws.appl[i] = keep;
-                ws.pre[i] = cnt;
-            }
-            __syncwarp();
-        }
-
-        // exclusive prefix sum of the per-pair successor counts
-        uint32_t carry = 0;
-        for (uint32_t base = 0; base < npairs; base += 32) {
-            uint32_t i = base + lane;
-            uint32_t v = i < npairs ? ws.pre[i] : 0u, incl = v;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t y = __shfl_up_sync(kFull, incl, o);
-                if (lane >= (uint32_t)o) incl += y;
-            }
-            if (i < npairs) ws.pre[i] = carry + incl - v;
-            carry += __shfl_sync(kFull, incl, 31);
-        }
-        if (lane == 0) ws.pre[npairs] = carry;
-        __syncwarp();
-
-        // C: one successor per lane per round, materialised by index, then looked up
-        for (uint32_t t0 = 0; t0 < carry; t0 += 32) {
-            uint32_t t = t0 + lane;
-            bool valid = t < carry;
-            K out;
-            uint32_t og = 0, omask = 0;
-            if (valid) {
-                uint32_t lo = 0, hi = npairs;
-                while (hi - lo > 1) {
-                    uint32_t mid = (lo + hi) >> 1;
-                    if (ws.pre[mid] <= t) lo = mid;
-                    else hi = mid;
-                }
-                uint32_t sub = t - ws.pre[lo];
-                og = lo / n;
-                uint32_t p = lo - og * n;
-                K key = ws.keys[og];
-                const uint32_t *rec = M.rec(p, KT<K>::get(key, M.fb(p), M.bs(p)));
-                uint32_t lcnt = (!filter || (ws.sel[og] >> p & 1u)) ? rec[R_LCNT] : 0u;
-                out = key;
-                if (sub < lcnt) {
-                    KT<K>::set(out, M.fb(p), M.bs(p), M.ltgt(rec[R_LOFF] + sub));
-                    omask = 1u << p;
-                } else {
-                    sub -= lcnt;
-                    uint32_t a = ws.appl[lo], roff = rec[R_ROFF];
-                    while (a) {
-                        uint32_t r = __ffs(a) - 1;
-                        a &= a - 1;
-                        uint32_t k = M.lrule(roff + r), mask = M.rmask(k), act = M.ract(k);
-                        uint32_t psz = product_size(key, mask, act);
-                        if (sub >= psz) {
-                            sub -= psz;
-                            continue;
-                        }
-                        uint32_t rest = mask;
-                        while (rest) {
-                            uint32_t q = __ffs(rest) - 1;
-                            rest &= rest - 1;
-                            const uint32_t *grp = M.group(M.rec(q, KT<K>::get(key, M.fb(q), M.bs(q))), act);
-                            uint32_t tc = grp[2], d = sub % tc;
-                            sub /= tc;
-                            KT<K>::set(out, M.fb(q), M.bs(q), M.stgt(grp[1] + d));
-                        }
-                        omask = mask;
-                        break;
-                    }
-                }
-            }
-            if (MODE == MODE_PROVISO && decide) {
-                if (valid) {
-                    st.lookups++;
-                    // cycle proviso: a successor satisfies it unless it is an explored
-                    // ("OLD") state -- every state in the table during this pass
-                    if (!find_key<K>(table, P.nbuckets, out, KT<K>::hash(out, P.seed), st.probes))
-                        atomicOr(&ws.prov[og], omask);
-                }
-                continue;
-            }
-            int res = -1;
-            if (valid) {
-                st.lookups++;
-                st.ilookups++;
-                res = find_or_insert<K>(table, P.nbuckets, out, KT<K>::hash(out, P.seed), st.probes);
-                if (res == 2) set_error(P.ctrl, GPX_ERR_TABLE_FULL);
-            }
-            uint32_t ins = __ballot_sync(kFull, res == 1);
-            if (ins) {
-                if (res == 1) {
-                    ws.stage[(shead + scount + __popc(ins & lanemask_lt)) % kStage] = out;
-                    st.inserts++;
-                }
-                scount += __popc(ins);
-                __syncwarp();
-                if (scount >= 32) stage_flush(32);
-            }
-        }
-
-        if (MODE == MODE_PROVISO && decide) {
-            __syncwarp();
-            select_clusters(B);
-            if (lane < B) P.sel[lvl_off + lane] = ws.sel[lane];
-        }
-        __syncwarp();
-    }
-
-    // Smallest valid cluster per state (GPUexplore.cu:1633-1672); ws.prov holds
-    // the proviso bits, ws.cl0 the static clusters.
-    __device__ void select_clusters(uint32_t B) {
-        if (MODE == MODE_PLAIN) return;
-        const uint32_t n = M.n;
-        __syncwarp();
-        const uint32_t npairs = B * n;
-        for (uint32_t i = lane; i < npairs; i += 32) {
-            uint32_t g = i / n, p = i - g * n;
-            uint32_t prov = ws.prov[g];
-            const uint32_t *cl = ws.cl0 + g * n;
-            uint32_t cp = (prov >> p & 1u) ? cl[p] : (cl[p] & ~(1u << p));
-            uint32_t closure = cp, todo = cp, valid = 0;
-            while (todo) {
-                uint32_t q = __ffs(todo) - 1;
-                todo &= ~(1u << q);
-                uint32_t cq = (prov >> q & 1u) ? cl[q] : (cl[q] & ~(1u << q));
-                valid |= (cq >> q) & 1u;
-                todo |= cq & ~closure & ~(1u << q);
-                closure |= cq;
-            }
-            ws.clo[i] = closure;
-            if (valid && closure) atomicMin(&ws.best[g], ((uint32_t)__popc(closure) << 5) | p);
-        }
-        __syncwarp();
-        if (lane < B) {
-            uint32_t b = ws.best[lane];
-            uint32_t all = (n == 32) ? kFull : ((1u << n) - 1u);
-            ws.sel[lane] = (b == kFull || (b >> 5) >= n) ? all : ws.clo[lane * n + (b & 31u)];
-        }
-        __syncwarp();
-    }
-
-    __device__ void flush_stats() {
-        if (scount) stage_flush(scount);
-        Ctrl *c = P.ctrl;
-        unsigned int v[5] = {st.lookups, st.probes, st.inserts, st.expanded, st.ilookups};
-#pragma unroll
-        for (int k = 0; k < 5; k++)
-            for (int o = 16; o; o >>= 1) v[k] += __shfl_xor_sync(kFull, v[k], o);
-        unsigned int viol = __any_sync(kFull, st.violation);
-        if (lane == 0) {
-            if (v[0]) atomicAdd(&c->lookups, (unsigned long long)v[0]);
-            if (v[1]) atomicAdd(&c->probes, (unsigned long long)v[1]);
-            if (v[2]) atomicAdd(&c->inserts, (unsigned long long)v[2]);
-            if (v[3]) atomicAdd(&c->expanded, (unsigned long long)v[3]);
-            if (v[4]) atomicAdd(&c->inserts_lookups, (unsigned long long)v[4]);
-            if (viol) atomicOr(&c->violation, 1u);
-        }
-        st = WarpStats{0, 0, 0, 0, 0, 0};
-    }
-};
 
 template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_kernel(Params P) {
     extern __shared__ __align__(16) unsigned char smem[];

@@ -81,3 +81,9 @@ std::string parse_gpf_words(const uint32_t *w, size_t n, Gpf *out);
 std::string decode_gpf(const Gpf &g, Decoded *out);
 
 } // namespace gpx
+
+// The opaque model handle of the C ABI (include/gpx.h).
+struct gpx_model {
+    gpx::Gpf gpf;
+    gpx::Decoded dec;
+};

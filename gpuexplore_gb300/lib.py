@@ -26,7 +26,7 @@ EXPORTS = [
     "gpx_model_load_file", "gpx_model_from_words", "gpx_model_info_get", "gpx_model_free", "gpx_explore",
     "gpx_explorer_create", "gpx_explorer_run", "gpx_explorer_set_model", "gpx_explorer_destroy",
     "gpx_result_free", "gpx_explorer_dump", "gpx_explore_noalloc", "gpx_random_gather_probe",
-    "gpx_selftest_bounded_wait",
+    "gpx_selftest_bounded_wait", "gpx_batch_options_init", "gpx_batch_job_init", "gpx_batch_explore",
 ]
 
 
@@ -50,6 +50,37 @@ class Result(C.Structure):
         ("expanded", C.c_uint64), ("kernel_ms", C.c_double), ("states_buf", C.POINTER(C.c_uint32)),
         ("table_slots", C.c_uint64), ("slot_bytes", C.c_uint32), ("blocks", C.c_uint32), ("threads", C.c_uint32),
         ("inserts", C.c_uint64),
+    ]
+
+
+class BatchJob(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32), ("property", C.c_int32), ("por", C.c_int32), ("cycle_proviso", C.c_int32),
+        ("max_states", C.c_uint64), ("capacity", C.c_uint64),
+    ]
+
+
+class BatchItem(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32), ("stopped", C.c_int32), ("verdict", C.c_int32), ("nlevels", C.c_uint32),
+        ("states", C.c_uint64), ("set_hash", C.c_uint64), ("capacity", C.c_uint64),
+        ("completion_ms", C.c_double), ("admissions", C.c_uint32), ("reserved", C.c_uint32),
+    ]
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32), ("device", C.c_int32), ("blocks", C.c_int32), ("threads", C.c_int32),
+        ("claim", C.c_int32), ("kernel_iters", C.c_int32), ("autotune", C.c_int32), ("max_admissions", C.c_int32),
+        ("load_factor", C.c_double), ("seed", C.c_uint64),
+    ]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [
+        ("device_ms", C.c_double), ("states", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+        ("launches", C.c_uint32), ("claim", C.c_int32), ("threads", C.c_int32), ("blocks", C.c_int32),
+        ("load_factor", C.c_double), ("tune_ms", C.c_double),
     ]
 
 
@@ -107,6 +138,13 @@ def load(path: str = LIB) -> C.CDLL:
                                         C.POINTER(Result)]
     lib.gpx_random_gather_probe.argtypes = [i, C.c_uint64, C.POINTER(C.c_double)]
     lib.gpx_selftest_bounded_wait.argtypes = [i, C.c_uint64, C.POINTER(C.c_uint64)]
+    lib.gpx_batch_options_init.argtypes = [C.POINTER(BatchOptions)]
+    lib.gpx_batch_options_init.restype = None
+    lib.gpx_batch_job_init.argtypes = [C.POINTER(BatchJob)]
+    lib.gpx_batch_job_init.restype = None
+    lib.gpx_batch_explore.argtypes = [C.POINTER(vp), C.POINTER(BatchJob), C.c_uint32, C.POINTER(BatchOptions),
+                                      C.POINTER(BatchItem), C.POINTER(C.c_uint64), C.c_uint32,
+                                      C.POINTER(BatchStats)]
     _lib = lib
     return lib
 
@@ -296,6 +334,44 @@ def selftest_bounded_wait(timeout_ns: int, device: int = 0):
     w = C.c_uint64()
     rc = load().gpx_selftest_bounded_wait(device, timeout_ns, C.byref(w))
     return rc, w.value
+
+
+def batch_explore(models: Sequence[Model], jobs: Sequence[Dict], level_capacity: int = 256,
+                  check: bool = True, **opts):
+    """gpx_batch_explore over `models` with one job dict per model (keys: property,
+    por, cycle_proviso, max_states, capacity).  Returns (items, stats)."""
+    lib = load()
+    n = len(models)
+    hs = (C.c_void_p * n)(*[m.handle.value for m in models])
+    js = (BatchJob * n)()
+    for k, j in enumerate(jobs):
+        lib.gpx_batch_job_init(C.byref(js[k]))
+        for key, v in j.items():
+            if key == "property" and isinstance(v, str):
+                v = PROPERTIES[v]
+            setattr(js[k], key, int(v))
+    o = BatchOptions()
+    lib.gpx_batch_options_init(C.byref(o))
+    for key, v in opts.items():
+        setattr(o, key, float(v) if key == "load_factor" else int(v))
+    items = (BatchItem * n)()
+    levels = (C.c_uint64 * (n * level_capacity))()
+    st = BatchStats()
+    rc = lib.gpx_batch_explore(hs, js, n, C.byref(o), items, levels, level_capacity, C.byref(st))
+    if check and rc != GPX_OK:
+        raise GpxError(rc, "batch exploration")
+    out = []
+    for k in range(n):
+        it = items[k]
+        nl = min(it.nlevels, level_capacity)
+        out.append({"status": it.status, "stopped": STOPS[it.stopped] if 0 <= it.stopped < 4 else str(it.stopped),
+                    "verdict": VERDICTS.get(it.verdict, str(it.verdict)), "states": it.states,
+                    "levels": [int(levels[k * level_capacity + l]) for l in range(nl)], "nlevels": it.nlevels,
+                    "set_hash": f"{it.set_hash:016x}", "capacity": it.capacity,
+                    "completion_ms": it.completion_ms, "admissions": it.admissions})
+    stats = {f: getattr(st, f) for f, _ in BatchStats._fields_}
+    stats["rc"] = rc
+    return out, stats
 
 
 def device_info(device: int = 0) -> Optional[DeviceInfo]:

@@ -196,6 +196,66 @@ int gpx_random_gather_probe(int device, uint64_t bytes, double *gathers_per_s);
 int gpx_explore_noalloc(const gpx_model *model, const gpx_options *opts, uint64_t *level_counts,
                         uint32_t level_capacity, gpx_result *result);
 
+/* ---- Batched exploration (no reference counterpart: the reference explores one
+ * network per process).  Many networks of uneven size explored in one
+ * persistent launch; each has its own hash-table and state-store partition,
+ * sized from an admission estimate, and its own BFS levels, closed by whichever
+ * warp finishes a level's last work claim (no grid-wide barrier).  An instance
+ * that overflows its partition is re-admitted in a later launch with four times
+ * the capacity.  Results per instance equal gpx_explore's on the same network. */
+typedef struct {
+    uint32_t struct_size;
+    int32_t property;       /* gpx_property */
+    int32_t por;            /* 0: none, 1: cluster POR */
+    int32_t cycle_proviso;
+    uint64_t max_states;    /* state budget (0 = none) */
+    uint64_t capacity;      /* states admitted (table + store partition); 0 = estimate */
+} gpx_batch_job;
+
+typedef struct {
+    int32_t status;         /* gpx_status of this instance */
+    int32_t stopped;        /* gpx_stop */
+    int32_t verdict;        /* violated gpx_property or GPX_PROP_NONE */
+    uint32_t nlevels;
+    uint64_t states;
+    uint64_t set_hash;      /* order-independent hash of the visited set */
+    uint64_t capacity;      /* states admitted in the launch that finished it */
+    double completion_ms;   /* device time from that launch's start to the instance's last level */
+    uint32_t admissions;    /* launches the instance needed */
+    uint32_t reserved;
+} gpx_batch_item;
+
+typedef struct {
+    uint32_t struct_size;
+    int32_t device;
+    int32_t blocks;         /* 0: every SM at full occupancy */
+    int32_t threads;        /* per block; 0 = 256 */
+    int32_t claim;          /* states per work claim (the frontier tile); 0 = 64 */
+    int32_t kernel_iters;   /* work claims per warp per launch (0 = until every instance is done) */
+    int32_t autotune;       /* choose claim, threads and load factor on a sample of the batch first */
+    int32_t max_admissions; /* launches per instance before an overflow is final (0 = 3) */
+    double load_factor;     /* table slots = admitted states / load_factor (0 = 0.5) */
+    uint64_t seed;
+} gpx_batch_options;
+
+typedef struct {
+    double device_ms;       /* device time of all batch launches, autotuning excluded */
+    uint64_t states;        /* states of all instances */
+    double p50_ms, p99_ms;  /* per-instance completion times (first launch) */
+    uint32_t launches;
+    int32_t claim, threads, blocks;
+    double load_factor;
+    double tune_ms;         /* host time spent autotuning */
+} gpx_batch_stats;
+
+void gpx_batch_options_init(gpx_batch_options *opts);
+void gpx_batch_job_init(gpx_batch_job *job);
+/* models[count], jobs[count], items[count]; level_counts (optional) receives
+ * count x level_capacity per-level counts, row i for instance i. */
+int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs, uint32_t count,
+                      const gpx_batch_options *opts, gpx_batch_item *items, uint64_t *level_counts,
+                      uint32_t level_capacity, gpx_batch_stats *stats);
+
 /* Write the visited set of the last run in the reference's --dump format
  * (print_local_queue, GPUexplore.cu:594-612): one state per line, local states
  * comma separated, then the stripped state-vector words. */

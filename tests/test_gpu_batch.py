@@ -1,0 +1,76 @@
+"""Batched exploration (many networks, one persistent launch) against the
+oracle, instance by instance."""
+import random
+
+import pytest
+
+from gpuexplore_gb300 import gen
+from helpers import FLAGS, oracle, write_net
+
+pytestmark = pytest.mark.gpu
+
+FLAGSET = ["plain", "deadlock", "safety", "por", "por_proviso", "por_safety"]
+
+
+def _batch_cases(n, seed):
+    rng = random.Random(seed)
+    cases = []
+    for k in range(n):
+        fam = rng.choice(["ring", "rand", "rand", "clus"])
+        if fam == "ring":
+            net = gen.ring(rng.randrange(100))
+        elif fam == "rand":
+            net = gen.random_network(rng.randrange(1000), nprocs=rng.randint(4, 14), states=(3, rng.randint(4, 9)),
+                                     outdeg=(1, rng.randint(2, 3)))
+        else:
+            net = gen.clustered(rng.randrange(1000), nprocs=rng.randint(6, 16), nclusters=(2, 4))
+        fs = rng.choice(FLAGSET)
+        budget = rng.choice([0, 2000, 50_000])
+        cases.append((net, fs, budget))
+    return cases
+
+
+def _check(lib, tmp_path, cases, **opts):
+    models, jobs, want = [], [], []
+    for k, (net, fs, budget) in enumerate(cases):
+        path = write_net(net, tmp_path, f"b{k}")
+        cli, kw = FLAGS[fs]
+        job = {"property": kw.get("property", "none"), "por": kw.get("por", 0),
+               "cycle_proviso": kw.get("cycle_proviso", 0), "max_states": budget or 400_000}
+        want.append(oracle(path, cli, max_states=job["max_states"]))
+        models.append(lib.Model.from_file(path))
+        jobs.append(job)
+    items, stats = lib.batch_explore(models, jobs, **opts)
+    for k, (it, w) in enumerate(zip(items, want)):
+        assert it["status"] == 0, (k, it)
+        for key in ("states", "levels", "verdict", "stopped", "set_hash"):
+            assert it[key] == w[key], (k, cases[k][1], key, it[key], w[key])
+    assert stats["states"] == sum(w["states"] for w in want)
+    return items, stats
+
+
+def test_batch_matches_oracle(gpu, tmp_path):
+    _check(gpu, tmp_path, _batch_cases(40, 1))
+
+
+def test_batch_readmission(gpu, tmp_path):
+    """Partitions admitted too small overflow and are re-admitted with 4x capacity."""
+    cases = _batch_cases(12, 2)
+    lib = gpu
+    models = []
+    for k, (net, fs, budget) in enumerate(cases):
+        models.append(lib.Model.from_file(write_net(net, tmp_path, f"r{k}")))
+    jobs = [{"max_states": 20_000, "capacity": 64} for _ in cases]
+    items, stats = lib.batch_explore(models, jobs, max_admissions=6)
+    for k, it in enumerate(items):
+        w = oracle(str(tmp_path / f"r{k}.gpf"), [], max_states=20_000)
+        assert it["status"] == 0 and it["states"] == w["states"] and it["set_hash"] == w["set_hash"]
+    assert max(it["admissions"] for it in items) > 1
+
+
+def test_batch_launch_shapes_and_autotune(gpu, tmp_path):
+    cases = _batch_cases(16, 3)
+    _check(gpu, tmp_path, cases, claim=32, threads=128, kernel_iters=8)
+    items, stats = _check(gpu, tmp_path, cases, autotune=1)
+    assert stats["claim"] in (32, 64, 128, 256) and stats["tune_ms"] > 0
+    assert stats["p99_ms"] >= stats["p50_ms"] > 0
