@@ -169,6 +169,103 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_other_workload(args, local):
+    """Configs 1, 3 and 5 (the headline is config 2): one JSON line each."""
+    import random
+    from gpuexplore_gb300 import build, gen, gpf, lib
+    build.build_all()
+    line = {"metric": "new states/s", "unit": "states/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded gpf generator)"}
+    if args.workload == "config4":
+        import time as _t
+        from gpuexplore_gb300 import learned_por
+        t0 = _t.time()
+        rows = learned_por.log_candidates(range(1, args.train_seeds + 1), budget=20_000, sample_every=128,
+                                          device=local)
+        t1 = _t.time()
+        # validation seeds (disjoint from training and evaluation) pick the training target
+        val = range(500_001, 500_001 + args.val_seeds)
+        model, target, loss, val_scores = learned_por.choose_target(rows, val, budget=args.eval_budget,
+                                                                    device=local)
+        t2 = _t.time()
+        held = range(1_000_001, 1_000_001 + args.eval_seeds)
+        ev = learned_por.evaluate(model, held, budget=args.eval_budget, device=local)
+        t3 = _t.time()
+        model_path = os.path.join(ROOT, "gpuexplore_gb300", "_lib", "por_model_config2.bin")
+        learned_por.save(model, model_path)
+        red = 1.0 - ev["decided_states_learned"] / max(1, ev["decided_states_cample"])
+        line.update(metric="states-to-verdict reduction vs plain cample", value=red, unit="fraction",
+                    higher_is_better=True, ms_per_step=1000 * (t3 - t0),
+                    config={"workload": f"config-4 learned cluster proposal: trained on candidate logs of "
+                                        f"{args.train_seeds} config-2 seeds, target chosen on {args.val_seeds} "
+                                        f"validation seeds, evaluated on {args.eval_seeds} held-out seeds with -p "
+                                        f"(cycle proviso), budget {args.eval_budget}; value = 1 - states to the "
+                                        f"verdict (learned / plain cample) on the seeds BFS decides",
+                            "rows": int(len(rows)), "target": target, "val_decided_states": val_scores,
+                            "train_loss": loss, "log_s": t1 - t0, "train_s": t2 - t1, "eval_s": t3 - t2,
+                            **{k: v for k, v in ev.items() if k != "per_seed"}})
+        print(json.dumps(line), flush=True)
+        return
+    if args.workload in ("config1", "config3"):
+        if args.workload == "config1":
+            nets = [gen.ring(s) for s in range(1, 11)]
+            kw = dict(property="deadlock", q_words=1 << 22)
+            desc = "config-1 rings of 8 processes x 5 states, seeds 1-10, -d, 2^22-word table"
+        else:
+            nets = [gen.clustered(s, nprocs=24) for s in range(1, 4)]
+            kw = dict(por=1, cycle_proviso=1, q_words=2_500_000_000, max_states=min(args.budget, 20_000_000))
+            desc = "config-3 clustered networks (24 processes, 4-6 clusters), seeds 1-3, --por --cycle-proviso"
+        models = [lib.Model.from_words(gpf.encode(n)) for n in nets]
+        ex = lib.Explorer(models[0], lib.options(device=local, **kw))
+        for _ in range(args.warmup):
+            for m in models:
+                ex.set_model(m)
+                ex.run()
+        ms, states, kms = 0.0, 0, 0.0
+        for _ in range(args.steps):
+            for m in models:
+                ex.set_model(m)
+                r = ex.run()
+                ms += r["setup_ms"] + r["kernel_ms"]
+                kms += r["kernel_ms"]
+                states += r["states"]
+        line.update(value=states / (ms / 1000.0), ms_per_step=ms / args.steps,
+                    config={"workload": desc, "states_per_step": states // args.steps, "networks": len(nets),
+                            "kernel_ms_per_step": kms / args.steps})
+    else:
+        rng = random.Random(5)
+        nets = gen.batch(5, count=args.batch_count)
+        models = [lib.Model.from_words(gpf.encode(n)) for n in nets]
+        jobs = []
+        for k in range(len(nets)):
+            jobs.append({"property": "deadlock" if k % 2 == 0 else "safety",
+                         "por": 1 if (k // 2) % 2 else 0, "cycle_proviso": 1 if (k // 2) % 2 else 0,
+                         "max_states": int(10 ** rng.uniform(3, 7))})
+        # the warm-up call autotunes claim size, block size and load factor; timed calls reuse them
+        tuned = {}
+        for w in range(max(1, args.warmup)):
+            _, st = lib.batch_explore(models, jobs, autotune=1 if w == 0 else 0, **tuned)
+            tuned = {"claim": st["claim"], "threads": st["threads"], "load_factor": st["load_factor"]}
+        dev, states, p50, p99 = 0.0, 0, [], []
+        for _ in range(args.steps):
+            items, st = lib.batch_explore(models, jobs, **tuned)
+            dev += st["device_ms"]
+            states += st["states"]
+            p50.append(st["p50_ms"])
+            p99.append(st["p99_ms"])
+        line.update(value=states / (dev / 1000.0), ms_per_step=dev / args.steps,
+                    config={"workload": f"config-5 batch of {len(nets)} random networks (4-24 procs x 4-32 states), "
+                                        "state budgets log-uniform 1e3-1e7, half -d / half -p, half cluster POR with "
+                                        "the cycle proviso, one persistent launch",
+                            "states_per_step": states // args.steps, "p50_ms": statistics.median(p50),
+                            "p99_ms": statistics.median(p99), "claim": st["claim"], "threads": st["threads"],
+                            "load_factor": st["load_factor"], "tune_ms": st["tune_ms"],
+                            "admissions_max": max(it["admissions"] for it in items),
+                            "failed": sum(1 for it in items if it["status"] != 0)})
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -180,6 +277,13 @@ def main():
                     help="state budget (smaller values give the profiling cases of the same network)")
     ap.add_argument("--q-words", type=int, default=Q_WORDS, help="hash table size in 32-bit words")
     ap.add_argument("--store-states", type=int, default=0, help="state store capacity (0: table slots)")
+    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3", "config4", "config5"],
+                    help="config2 is the headline; the others print their own line")
+    ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--train-seeds", type=int, default=2000)
+    ap.add_argument("--eval-seeds", type=int, default=200)
+    ap.add_argument("--val-seeds", type=int, default=60)
+    ap.add_argument("--eval-budget", type=int, default=2_000_000)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -191,6 +295,12 @@ def main():
         dist.init_process_group("gloo")
     if args.impl == "reference":
         run_reference(args, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload != "config2":
+        if rank == 0:
+            run_other_workload(args, local)
         if dist:
             dist.destroy_process_group()
         return

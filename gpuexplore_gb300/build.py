@@ -61,7 +61,8 @@ def _run_parallel(cmds: List[List[str]]) -> None:
 def build_library(force: bool = False) -> str:
     """Compile libgpx.so and the gpuexplore tool; returns the library path."""
     os.makedirs(LIBDIR, exist_ok=True)
-    srcs_cu = [os.path.join(CSRC, "gpx_explore.cu"), os.path.join(CSRC, "gpx_batch.cu")]
+    srcs_cu = [os.path.join(CSRC, "gpx_explore.cu"), os.path.join(CSRC, "gpx_batch.cu"),
+               os.path.join(CSRC, "gpx_por.cu")]
     srcs_cpp = [os.path.join(CSRC, "gpx_model.cpp")]
     headers = [os.path.join(INCLUDE, "gpx.h"), os.path.join(CSRC, "gpx_model.h"),
                os.path.join(CSRC, "gpx_device.cuh")]
@@ -88,7 +89,7 @@ def build_oracle(force: bool = False) -> str:
     os.makedirs(ORACLE_BUILD, exist_ok=True)
     src = os.path.join(ORACLE_DIR, "gpx_oracle.c")
     if force or _stale(ORACLE, [src]):
-        _run_parallel([["gcc", "-O2", "-fopenmp", "-std=gnu11", src, "-o", ORACLE]])
+        _run_parallel([["gcc", "-O2", "-fopenmp", "-std=gnu11", src, "-o", ORACLE, "-lm"]])
     return ORACLE
 
 

@@ -37,6 +37,7 @@ static const char *kHelp =
     "  --max-states NUM   Stop at the end of the BFS level that reaches NUM states\n"
     "  --store NUM        Capacity of the state store in states\n"
     "  --device NUM       CUDA device to use\n"
+    "  --por-model FILE   Use the learned cluster proposal in FILE (a gpx_por_model) with --por\n"
     "  -h, --help         Show this help message\n";
 
 static uint64_t mix64(uint64_t z) {
@@ -60,6 +61,7 @@ int main(int argc, char **argv) {
     gpx_options o;
     gpx_options_init(&o);
     const char *dump_file = nullptr;
+    const char *por_model_file = nullptr;
     int i = 2;
     auto need = [&](int k) {
         if (k + 1 >= argc) {
@@ -120,6 +122,9 @@ int main(int argc, char **argv) {
         } else if (!strcmp(a, "--device")) {
             o.device = atoi(need(i));
             i += 2;
+        } else if (!strcmp(a, "--por-model")) {
+            por_model_file = need(i);
+            i += 2;
         } else {
             fprintf(stderr, "ERROR: unrecognized option %s\n", a);
             fputs(kHelp, stdout);
@@ -166,12 +171,23 @@ int main(int argc, char **argv) {
     printf("max. grid size: %d\n", dev.max_grid_size);
     printf("nr. of multiprocessors: %d\n", dev.sm_count);
 
+    gpx_por_model pm;
+    if (por_model_file) {
+        FILE *pf = fopen(por_model_file, "rb");
+        if (!pf || fread(&pm, sizeof pm, 1, pf) != 1) {
+            fprintf(stderr, "ERROR: cannot read POR model %s\n", por_model_file);
+            return 1;
+        }
+        fclose(pf);
+        if (o.por) o.por = 2;
+    }
     gpx_explorer *ex = nullptr;
     rc = gpx_explorer_create(m, &o, &ex);
     if (rc != GPX_OK) {
         fprintf(stderr, "ERROR: %s\n", gpx_status_string(rc));
         return 1;
     }
+    if (por_model_file) gpx_explorer_set_por_model(ex, &pm);
     // hash constants derived from the seed (the reference draws 16 with rand(), GPUexplore.cu:1990-1993)
     auto explore_start = std::chrono::steady_clock::now();
     gpx_result r;

@@ -50,6 +50,7 @@ struct __align__(128) BInst {
     unsigned long long *levels;
     unsigned long long max_states;
     uint32_t property, mode;
+    const gpx_por_model *por_model; // learned proposal (job por == 2), else null
 };
 
 struct BGlobal {
@@ -151,6 +152,8 @@ static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char 
     P.ctrl = &I->ctrl;
     P.seed = BP.seed;
     P.property = I->property;
+    P.por_model = I->por_model;
+    P.learned = I->por_model ? 1u : 0u;
     Explorer<K128, MODE> E(P, I->model, *(WarpScratch<K128, MODE> *)raw);
     uint32_t B = kPairMax / E.M.n;
     B = B > 32 ? 32 : (B < 1 ? 1 : B);
@@ -301,7 +304,7 @@ struct Outcome {
 uint64_t estimate_capacity(const gpx_model *m, const gpx_batch_job &j) {
     double prod = 1;
     for (uint32_t ns : m->dec.nstates) prod *= ns;
-    double est = j.max_states ? (double)j.max_states * 8.0 : 4.0e6;
+    double est = j.max_states ? (double)j.max_states * 6.0 : 4.0e6; // a BFS level can overshoot the budget
     if (prod < est) est = prod * 1.05 + 64;
     if (est < 1024) est = 1024;
     return (uint64_t)est;
@@ -310,7 +313,8 @@ uint64_t estimate_capacity(const gpx_model *m, const gpx_batch_job &j) {
 // One launch (plus -k relaunches) over `idx` instances with the given capacities.
 int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, uint64_t seed,
                const gpx_model *const *models, const gpx_batch_job *jobs, const std::vector<uint32_t> &idx,
-               const std::vector<uint64_t> &cap, std::vector<Outcome> *out, float *device_ms, uint32_t *launches) {
+               const std::vector<uint64_t> &cap, const gpx_por_model *d_por, std::vector<Outcome> *out,
+               float *device_ms, uint32_t *launches) {
     int rc = GPX_OK;
     const uint32_t count = (uint32_t)idx.size();
     std::vector<BInst> h(count);
@@ -373,6 +377,7 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
     BCUDA(cudaMalloc(&d_inst, count * sizeof(BInst)));
     BCUDA(cudaMalloc(&d_g, sizeof(BGlobal)));
     for (uint32_t k = 0; k < count; k++) {
+        h[k].por_model = (jobs[idx[k]].por == 2) ? d_por : nullptr;
         h[k].table = (K128 *)(d_table + toff[k]);
         h[k].store = (K128 *)(d_store + soff[k]);
         h[k].sel = h[k].mode == MODE_PROVISO ? (uint32_t *)(d_sel + seloff[k]) : nullptr;
@@ -520,6 +525,24 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
         cap[i] = jobs[i].capacity ? jobs[i].capacity : estimate_capacity(models[i], jobs[i]);
         todo.push_back(i);
     }
+    // Admission: the estimates of one launch must fit in device memory (table at the
+    // load factor + store + cluster array per state); scale them down together if
+    // not -- instances that then overflow are re-admitted with more room.
+    {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return GPX_ERR_CUDA;
+        const double per_state = 16.0 / cfg.load_factor + 16.0 + 4.0;
+        double want = 0;
+        for (uint32_t i : todo) want += (double)cap[i] * per_state;
+        const double room = 0.7 * (double)free_b;
+        if (want > room)
+            for (uint32_t i : todo) cap[i] = std::max<uint64_t>(1024, (uint64_t)((double)cap[i] * room / want));
+    }
+    gpx_por_model *d_por = nullptr;
+    if (opts->por_model) {
+        if (cudaMalloc(&d_por, sizeof(gpx_por_model)) != cudaSuccess) return GPX_ERR_NOMEM;
+        cudaMemcpy(d_por, opts->por_model, sizeof(gpx_por_model), cudaMemcpyHostToDevice);
+    }
     // the request rate of random hash probes bounds these kernels: fetch one sector per L2 miss
     size_t saved_fetch = 0;
     bool restore = cudaDeviceGetLimit(&saved_fetch, cudaLimitMaxL2FetchGranularity) == cudaSuccess &&
@@ -545,7 +568,8 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
                     std::vector<Outcome> o;
                     float ms = 0;
                     uint32_t l = 0;
-                    if (run_launch(opts->device, prop, c, opts->seed, models, jobs, sample, scap, &o, &ms, &l) ==
+                    if (run_launch(opts->device, prop, c, opts->seed, models, jobs, sample, scap, d_por, &o, &ms,
+                                   &l) ==
                             GPX_OK &&
                         ms < best) {
                         best = ms;
@@ -560,10 +584,19 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
     std::vector<double> completion;
     for (int adm = 1; adm <= max_adm && !todo.empty(); adm++) {
         std::vector<uint64_t> c2;
-        for (uint32_t i : todo) c2.push_back(cap[i]);
+        {
+            size_t free_b = 0, total_b = 0;
+            cudaMemGetInfo(&free_b, &total_b);
+            const double per_state = 16.0 / cfg.load_factor + 16.0 + 4.0;
+            double want = 0;
+            for (uint32_t i : todo) want += (double)cap[i] * per_state;
+            const double room = 0.7 * (double)free_b;
+            double scale = want > room ? room / want : 1.0;
+            for (uint32_t i : todo) c2.push_back(std::max<uint64_t>(1024, (uint64_t)((double)cap[i] * scale)));
+        }
         std::vector<Outcome> out;
         float ms = 0;
-        rc = run_launch(opts->device, prop, cfg, opts->seed, models, jobs, todo, c2, &out, &ms, &st.launches);
+        rc = run_launch(opts->device, prop, cfg, opts->seed, models, jobs, todo, c2, d_por, &out, &ms, &st.launches);
         st.device_ms += ms;
         if (rc != GPX_OK && out.empty()) break;
         std::vector<uint32_t> again;
@@ -594,6 +627,7 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
         rc = GPX_OK;
     }
     if (restore) cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, saved_fetch);
+    if (d_por) cudaFree(d_por);
     for (uint32_t i = 0; i < count; i++) st.states += items[i].states;
     st.p50_ms = percentile(completion, 0.50);
     st.p99_ms = percentile(completion, 0.99);

@@ -61,6 +61,13 @@ struct Params {
     uint32_t property;
     uint32_t levels_per_launch;
     uint32_t total_warps;
+    // learned cluster proposal (por == 2) and candidate logging (decide pass)
+    const gpx_por_model *por_model;
+    uint32_t learned;
+    uint32_t log_every;
+    gpx_por_log_row *log;
+    unsigned long long *log_count;
+    unsigned long long log_cap;
 };
 
 // ------------------------------------------------------------- device helpers
@@ -294,7 +301,9 @@ template <class K, int MODE> struct WarpScratch {
     uint32_t en[32];             // per state: some transition enabled
     uint32_t cl0[kPor];          // per pair: static POR cluster
     uint32_t clo[kPor];          // per pair: cluster closure
-    uint32_t prov[32], sel[32], best[32];
+    uint32_t nw[kPor];           // per pair: successors not yet visited (decide pass, for the log)
+    uint32_t prov[32], sel[32], best[32], vmask[32];
+    unsigned long long lbest[32]; // learned proposal: (sortable score, popcount, process)
 };
 
 struct WarpStats {
@@ -345,6 +354,56 @@ static __device__ __forceinline__ bool wait_change(const unsigned int *word, uns
         if (globaltimer() - t0 > timeout_ns) return false;
     }
     return true;
+}
+
+// ------------------------------------------- learned cluster proposal helpers
+
+// Bucket of a (process, local state) pair among the 32 hashed one-hot features.
+static __host__ __device__ __forceinline__ uint32_t por_hash_bucket(uint32_t p, uint32_t s) {
+    uint32_t h = (p * 0x9E3779B1u) ^ (s * 0x85EBCA77u);
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    return h >> 27;
+}
+
+// d = c + sum_i a_i * b_i over the 4 bytes, a signed, b unsigned (exact).
+static __device__ __forceinline__ int dp4a_su(uint32_t a, uint32_t b, int c) {
+    int d;
+    asm("dp4a.s32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
+// Round a non-negative float to bfloat16 precision, to nearest, ties to even.
+static __host__ __device__ __forceinline__ float bf16_round(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    u &= 0xFFFF0000u;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+// MLP score of one candidate (features packed 4 per word, GPX_POR_FEATURES = 40).
+static __device__ float por_mlp_score(const gpx_por_model *m, const uint32_t (&xw)[10]) {
+    float out = 0.0f;
+    for (int k = 0; k < GPX_POR_HIDDEN; k++) {
+        const uint32_t *row = (const uint32_t *)m->w1[k];
+        int acc = 0;
+#pragma unroll
+        for (int j = 0; j < 10; j++) acc = dp4a_su(__ldg(row + j), xw[j], acc);
+        float h = fmaf((float)acc, __ldg(&m->s1[k]), __ldg(&m->b1[k]));
+        h = h > 0.0f ? h : 0.0f;
+        h = bf16_round(h);
+        out = fmaf((float)m->w2[k], h, out);
+    }
+    return fmaf(out, m->s2, m->b2);
+}
+
+// Order-preserving map of a float to an unsigned key.
+static __device__ __forceinline__ uint32_t float_key(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
 // ------------------------------------------------------------- the kernel
@@ -410,6 +469,10 @@ template <class K, int MODE> struct Explorer {
             ws.prov[lane] = 0;
             ws.best[lane] = kFull;
             ws.sel[lane] = kFull;
+            if (MODE != MODE_PLAIN) {
+                ws.vmask[lane] = 0;
+                ws.lbest[lane] = ~0ull;
+            }
         }
         __syncwarp();
         const uint32_t npairs = B * n;
@@ -452,7 +515,10 @@ template <class K, int MODE> struct Explorer {
             }
             ws.appl[i] = appl;
             ws.pre[i] = cnt;
-            if (MODE != MODE_PLAIN) ws.cl0[i] = rec[R_CL0];
+            if (MODE != MODE_PLAIN) {
+                ws.cl0[i] = rec[R_CL0];
+                ws.nw[i] = 0;
+            }
             if (lcnt | appl) ws.en[g] = 1;
             if (MODE == MODE_POR) atomicOr(&ws.prov[g], provbits);
             if (viol) st.violation = 1;
@@ -463,7 +529,7 @@ template <class K, int MODE> struct Explorer {
 
         // B: the cluster each state expands (POR); without the cycle proviso the
         //    proviso bits are plain enabledness (GPUexplore.cu:1395-1397)
-        if (MODE == MODE_POR) select_clusters(B);
+        if (MODE == MODE_POR) select_clusters(B, false);
         if (MODE == MODE_PROVISO && !decide) {
             if (lane < B) ws.sel[lane] = __ldcg(P.sel + lvl_off + lane);
             __syncwarp();
@@ -561,8 +627,10 @@ template <class K, int MODE> struct Explorer {
                     st.lookups++;
                     // cycle proviso: a successor satisfies it unless it is an explored
                     // ("OLD") state -- every state in the table during this pass
-                    if (!find_key<K>(table, P.nbuckets, out, KT<K>::hash(out, P.seed), st.probes))
+                    if (!find_key<K>(table, P.nbuckets, out, KT<K>::hash(out, P.seed), st.probes)) {
                         atomicOr(&ws.prov[og], omask);
+                        if (P.log) atomicAdd(&ws.nw[og * M.n + (__ffs(omask) - 1)], 1u);
+                    }
                 }
                 continue;
             }
@@ -587,15 +655,56 @@ template <class K, int MODE> struct Explorer {
 
         if (MODE == MODE_PROVISO && decide) {
             __syncwarp();
-            select_clusters(B);
+            select_clusters(B, true);
             if (lane < B) P.sel[lvl_off + lane] = ws.sel[lane];
         }
         __syncwarp();
     }
 
-    // Smallest valid cluster per state (GPUexplore.cu:1633-1672); ws.prov holds
-    // the proviso bits, ws.cl0 the static clusters.
-    __device__ void select_clusters(uint32_t B) {
+    // Successors generated by pair i's process (its local targets and the rules it
+    // leads); `prefix` when ws.pre already holds the exclusive prefix sum.
+    __device__ uint32_t pair_succ(uint32_t i, bool prefix) const { return prefix ? ws.pre[i + 1] - ws.pre[i] : ws.pre[i]; }
+
+    // Features of candidate closure C of state g (GPX_POR_FEATURES small integers,
+    // packed 4 per word): see include/gpx.h.
+    __device__ void cluster_features(uint32_t g, uint32_t C, bool prefix, uint32_t (&xw)[10], uint32_t &succ) const {
+        const uint32_t n = M.n;
+        const K key = ws.keys[g];
+        uint32_t x[GPX_POR_FEATURES];
+#pragma unroll
+        for (int j = 0; j < GPX_POR_FEATURES; j++) x[j] = 0;
+        uint32_t lt = 0, sc = 0, deg = 0, rl = 0;
+        uint32_t rest = C;
+        while (rest) {
+            uint32_t q = __ffs(rest) - 1;
+            rest &= rest - 1;
+            uint32_t sq = KT<K>::get(key, M.fb(q), M.bs(q));
+            lt += M.rec(q, sq)[R_LCNT];
+            sc += pair_succ(g * n + q, prefix);
+            deg += __popc(ws.cl0[g * n + q]);
+            rl += __popc(ws.appl[g * n + q]);
+            x[8 + por_hash_bucket(q, sq)]++;
+        }
+        succ = sc;
+        x[0] = __popc(C);
+        x[1] = lt < 255 ? lt : 255;
+        x[2] = sc < 255 ? sc : 255;
+        x[3] = deg < 255 ? deg : 255;
+        x[4] = __popc(C & ws.prov[g]);
+        x[5] = n;
+        x[6] = rl < 255 ? rl : 255;
+        x[7] = 1;
+#pragma unroll
+        for (int w = 0; w < 10; w++)
+            xw[w] = x[4 * w] | (x[4 * w + 1] << 8) | (x[4 * w + 2] << 16) | (x[4 * w + 3] << 24);
+    }
+
+    // Cluster per state (GPUexplore.cu:1633-1672): close each process's cluster
+    // (its own bit dropped when its proviso fails), keep closures with a member
+    // whose proviso holds, take the smallest (ties: lowest process; default: all)
+    // -- or, with the learned proposal, the lowest-scoring valid closure after the
+    // proposal passes the same checks.  ws.prov holds the proviso bits.
+    __device__ void select_clusters(uint32_t B, bool prefix) {
         if (MODE == MODE_PLAIN) return;
         const uint32_t n = M.n;
         __syncwarp();
@@ -615,13 +724,77 @@ template <class K, int MODE> struct Explorer {
                 closure |= cq;
             }
             ws.clo[i] = closure;
-            if (valid && closure) atomicMin(&ws.best[g], ((uint32_t)__popc(closure) << 5) | p);
+            if (valid && closure) {
+                atomicMin(&ws.best[g], ((uint32_t)__popc(closure) << 5) | p);
+                atomicOr(&ws.vmask[g], 1u << p);
+            }
         }
         __syncwarp();
+        const bool learn = P.learned && P.por_model;
+        const bool logging = (MODE == MODE_PROVISO) && P.log && prefix;
+        if (learn || logging) {
+            for (uint32_t i = lane; i < npairs; i += 32) {
+                uint32_t g = i / n, p = i - g * n;
+                if (!(ws.vmask[g] >> p & 1u)) continue;
+                uint32_t C = ws.clo[i];
+                bool first = true; // one entry per distinct closure of the state
+                for (uint32_t q = 0; q < p; q++)
+                    if ((ws.vmask[g] >> q & 1u) && ws.clo[g * n + q] == C) first = false;
+                if (!first) continue;
+                uint32_t xw[10], succ = 0;
+                cluster_features(g, C, prefix, xw, succ);
+                if (learn) {
+                    float sc = por_mlp_score(P.por_model, xw);
+                    if (isfinite(sc))
+                        atomicMin(&ws.lbest[g], ((unsigned long long)float_key(sc) << 32) |
+                                                     (((uint32_t)__popc(C) << 5) | p));
+                }
+                if (logging) {
+                    uint32_t tag = (uint32_t)KT<K>::hash(ws.keys[g], 0x5BD1E995ull);
+                    if (P.log_every && (tag % P.log_every) == 0) {
+                        unsigned long long slot = atomicAdd(P.log_count, 1ull);
+                        if (slot < P.log_cap) {
+                            gpx_por_log_row *row = P.log + slot;
+                            uint32_t nwsum = 0, rest = C;
+                            while (rest) {
+                                uint32_t q = __ffs(rest) - 1;
+                                rest &= rest - 1;
+                                nwsum += ws.nw[g * n + q];
+                            }
+                            for (int w = 0; w < 10; w++) ((uint32_t *)row->x)[w] = xw[w];
+                            row->succ = succ;
+                            row->new_succ = nwsum;
+                            row->state_tag = tag;
+                            row->popc = (uint8_t)__popc(C);
+                            uint32_t b = ws.best[g];
+                            row->cample_choice = (b != kFull && ws.clo[g * n + (b & 31u)] == C) ? 1 : 0;
+                            row->pad[0] = row->pad[1] = 0;
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+        }
         if (lane < B) {
             uint32_t b = ws.best[lane];
             uint32_t all = (n == 32) ? kFull : ((1u << n) - 1u);
-            ws.sel[lane] = (b == kFull || (b >> 5) >= n) ? all : ws.clo[lane * n + (b & 31u)];
+            uint32_t sel = (b == kFull || (b >> 5) >= n) ? all : ws.clo[lane * n + (b & 31u)];
+            if (learn && ws.lbest[lane] != ~0ull) {
+                // re-check the proposal: non-empty, closed under the members'
+                // clusters, and some member's proviso holds; else plain cample
+                uint32_t C = ws.clo[lane * n + (uint32_t)(ws.lbest[lane] & 31u)];
+                uint32_t prov = ws.prov[lane], rest = C;
+                bool closed = C != 0, some = (C & prov) != 0;
+                while (rest) {
+                    uint32_t q = __ffs(rest) - 1;
+                    rest &= rest - 1;
+                    uint32_t cq = ws.cl0[lane * n + q];
+                    if (!(prov >> q & 1u)) cq &= ~(1u << q);
+                    if (cq & ~C) closed = false;
+                }
+                if (closed && some) sel = C;
+            }
+            ws.sel[lane] = sel;
         }
         __syncwarp();
     }

@@ -146,8 +146,9 @@ template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_k
         bool decide = (MODE == MODE_PROVISO) && vload(&c->phase) == PH_DECIDE;
         unsigned long long nlev = hi - lo;
         for (;;) {
-            unsigned long long base = 0;
-            if (E.lane == 0) base = atomicAdd(&c->cursor, (unsigned long long)claim);
+            unsigned long long base = nlev;
+            // read before contending: on small levels most warps find nothing to claim
+            if (E.lane == 0 && vload(&c->cursor) < nlev) base = atomicAdd(&c->cursor, (unsigned long long)claim);
             base = __shfl_sync(kFull, base, 0);
             if (base >= nlev || vload(&c->error)) break;
             unsigned long long end = base + claim < nlev ? base + claim : nlev;
@@ -295,6 +296,12 @@ struct gpx_explorer {
     bool model_in_smem = false;
     unsigned long long last_count = 0, last_lo = 0, last_hi = 0;
     uint32_t bits_statevector = 0;
+    gpx_por_model *d_por_model = nullptr; // learned proposal (por == 2)
+    bool have_por_model = false;
+    gpx_por_log_row *d_log = nullptr;     // candidate log (decide pass)
+    unsigned long long *d_log_count = nullptr;
+    unsigned long long log_cap = 0;
+    uint32_t log_every = 0;
 };
 
 namespace {
@@ -378,6 +385,14 @@ Params make_params(gpx_explorer *ex) {
     P.property = (uint32_t)ex->property;
     P.levels_per_launch = ex->o.kernel_iters > 0 ? (uint32_t)ex->o.kernel_iters : 0;
     P.total_warps = (uint32_t)(ex->blocks * (ex->threads / 32));
+    P.learned = (ex->o.por == 2 && ex->have_por_model) ? 1u : 0u;
+    P.por_model = ex->have_por_model ? ex->d_por_model : nullptr;
+    if (ex->d_log && ex->log_cap && ex->mode == MODE_PROVISO) {
+        P.log = ex->d_log;
+        P.log_count = ex->d_log_count;
+        P.log_cap = ex->log_cap;
+        P.log_every = ex->log_every;
+    }
     return P;
 }
 
@@ -516,6 +531,9 @@ void gpx_explorer_destroy(gpx_explorer *ex) {
     if (ex->d_scalar) cudaFree(ex->d_scalar);
     if (ex->d_ctrl) cudaFree(ex->d_ctrl);
     if (ex->h_ctrl) cudaFreeHost(ex->h_ctrl);
+    if (ex->d_por_model) cudaFree(ex->d_por_model);
+    if (ex->d_log) cudaFree(ex->d_log);
+    if (ex->d_log_count) cudaFree(ex->d_log_count);
     for (auto &e : ex->ev)
         if (e) cudaEventDestroy(e);
     if (ex->st) cudaStreamDestroy(ex->st);
@@ -606,6 +624,7 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     c0.phase = ex->mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND;
     *ex->h_ctrl = c0;
     GPX_CUDA(cudaMemcpyAsync(ex->d_ctrl, ex->h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, ex->st));
+    if (ex->d_log_count) GPX_CUDA(cudaMemsetAsync(ex->d_log_count, 0, 8, ex->st));
     ex->ks.init<<<1, 32, 0, ex->st>>>(P);
     GPX_CUDA(cudaGetLastError());
     GPX_CUDA(cudaEventRecord(ex->ev[1], ex->st));
@@ -727,6 +746,46 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     ex->last_lo = c.lo;
     ex->last_hi = c.hi;
     return r->status;
+}
+
+int gpx_explorer_set_por_model(gpx_explorer *ex, const gpx_por_model *m) {
+    if (!ex) return GPX_ERR_INVALID;
+    if (!m) {
+        ex->have_por_model = false;
+        return GPX_OK;
+    }
+    if (!ex->d_por_model) GPX_CUDA(cudaMalloc(&ex->d_por_model, sizeof(gpx_por_model)));
+    GPX_CUDA(cudaMemcpy(ex->d_por_model, m, sizeof(gpx_por_model), cudaMemcpyHostToDevice));
+    ex->have_por_model = true;
+    return GPX_OK;
+}
+
+int gpx_explorer_set_por_log(gpx_explorer *ex, uint64_t capacity, uint32_t sample_every) {
+    if (!ex) return GPX_ERR_INVALID;
+    if (ex->d_log) cudaFree(ex->d_log);
+    ex->d_log = nullptr;
+    ex->log_cap = 0;
+    if (!capacity || !sample_every) return GPX_OK;
+    GPX_CUDA(cudaMalloc(&ex->d_log, capacity * sizeof(gpx_por_log_row)));
+    if (!ex->d_log_count) GPX_CUDA(cudaMalloc(&ex->d_log_count, 8));
+    GPX_CUDA(cudaMemset(ex->d_log_count, 0, 8));
+    ex->log_cap = capacity;
+    ex->log_every = sample_every;
+    return GPX_OK;
+}
+
+int gpx_explorer_get_por_log(gpx_explorer *ex, gpx_por_log_row *rows, uint64_t capacity, uint64_t *nrows) {
+    if (!ex || !nrows) return GPX_ERR_INVALID;
+    *nrows = 0;
+    if (!ex->d_log) return GPX_OK;
+    unsigned long long n = 0;
+    GPX_CUDA(cudaMemcpy(&n, ex->d_log_count, 8, cudaMemcpyDeviceToHost));
+    n = std::min<unsigned long long>(n, ex->log_cap);
+    *nrows = n;
+    if (rows && capacity)
+        GPX_CUDA(cudaMemcpy(rows, ex->d_log, std::min<unsigned long long>(n, capacity) * sizeof(gpx_por_log_row),
+                            cudaMemcpyDeviceToHost));
+    return GPX_OK;
 }
 
 int gpx_explore(const gpx_model *model, const gpx_options *opts, gpx_result *result) {

@@ -239,16 +239,23 @@ def clustered(seed: int, nprocs: int = 24, nclusters: Tuple[int, int] = (4, 6),
 
 
 def batch(seed: int, count: int = 512, procs: Tuple[int, int] = (4, 24),
-          states: Tuple[int, int] = (4, 32)) -> List[Network]:
-    """`count` random networks of uneven sizes (process counts and local state
-    counts drawn per network)."""
+          states: Tuple[int, int] = (4, 32), max_bits: int = 126) -> List[Network]:
+    """`count` random networks of uneven sizes: per network a process count in
+    `procs` and an upper bound on local states in `states`; networks whose state
+    vector would exceed `max_bits` are redrawn with fewer states per process.
+    Every network carries the safety monitor, so the same network can be checked
+    for deadlocks or for the embedded safety property."""
     rng = random.Random(seed)
     nets = []
     for _ in range(count):
         n = rng.randint(procs[0], procs[1])
         hi = rng.randint(states[0], states[1])
-        nets.append(random_network(rng.randrange(1 << 30), nprocs=n, states=(states[0], hi),
-                                   outdeg=(1, 3), safety=rng.random() < 0.5))
+        while True:
+            net = random_network(rng.randrange(1 << 30), nprocs=n, states=(states[0], hi), outdeg=(1, 3))
+            if net.firstbit()[-1] <= max_bits or hi <= states[0]:
+                break
+            hi = max(states[0], hi // 2)
+        nets.append(net)
     return nets
 
 

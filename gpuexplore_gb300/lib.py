@@ -27,7 +27,41 @@ EXPORTS = [
     "gpx_explorer_create", "gpx_explorer_run", "gpx_explorer_set_model", "gpx_explorer_destroy",
     "gpx_result_free", "gpx_explorer_dump", "gpx_explore_noalloc", "gpx_random_gather_probe",
     "gpx_selftest_bounded_wait", "gpx_batch_options_init", "gpx_batch_job_init", "gpx_batch_explore",
+    "gpx_explorer_set_por_model", "gpx_explorer_set_por_log", "gpx_explorer_get_por_log",
+    "gpx_train_options_init", "gpx_por_train", "gpx_por_grad",
 ]
+
+POR_F, POR_H = 40, 64
+
+
+class PorModel(C.Structure):
+    """gpx_por_model: int8 w1[64][40], s1[64], b1[64], int8 w2[64], s2, b2."""
+    _fields_ = [("w1", (C.c_int8 * POR_F) * POR_H), ("s1", C.c_float * POR_H), ("b1", C.c_float * POR_H),
+                ("w2", C.c_int8 * POR_H), ("s2", C.c_float), ("b2", C.c_float)]
+
+    def to_bytes(self) -> bytes:
+        return bytes(memoryview(self))
+
+    @classmethod
+    def from_bytes(cls, b: bytes) -> "PorModel":
+        m = cls()
+        C.memmove(C.addressof(m), b, C.sizeof(cls))
+        return m
+
+
+class PorLogRow(C.Structure):
+    _fields_ = [("x", C.c_uint8 * POR_F), ("succ", C.c_uint32), ("new_succ", C.c_uint32), ("state_tag", C.c_uint32),
+                ("popc", C.c_uint8), ("cample_choice", C.c_uint8), ("pad", C.c_uint8 * 2)]
+
+
+POR_LOG_DTYPE = np.dtype([("x", np.uint8, (POR_F,)), ("succ", np.uint32), ("new_succ", np.uint32),
+                          ("state_tag", np.uint32), ("popc", np.uint8), ("cample_choice", np.uint8),
+                          ("pad", np.uint8, (2,))])
+
+
+class TrainOptions(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("device", C.c_int32), ("epochs", C.c_uint32), ("batch", C.c_uint32),
+                ("lr", C.c_float), ("weight_decay", C.c_float), ("seed", C.c_uint64)]
 
 
 class Options(C.Structure):
@@ -72,7 +106,7 @@ class BatchOptions(C.Structure):
     _fields_ = [
         ("struct_size", C.c_uint32), ("device", C.c_int32), ("blocks", C.c_int32), ("threads", C.c_int32),
         ("claim", C.c_int32), ("kernel_iters", C.c_int32), ("autotune", C.c_int32), ("max_admissions", C.c_int32),
-        ("load_factor", C.c_double), ("seed", C.c_uint64),
+        ("load_factor", C.c_double), ("seed", C.c_uint64), ("por_model", C.c_void_p),
     ]
 
 
@@ -138,6 +172,15 @@ def load(path: str = LIB) -> C.CDLL:
                                         C.POINTER(Result)]
     lib.gpx_random_gather_probe.argtypes = [i, C.c_uint64, C.POINTER(C.c_double)]
     lib.gpx_selftest_bounded_wait.argtypes = [i, C.c_uint64, C.POINTER(C.c_uint64)]
+    lib.gpx_explorer_set_por_model.argtypes = [vp, C.POINTER(PorModel)]
+    lib.gpx_explorer_set_por_log.argtypes = [vp, C.c_uint64, C.c_uint32]
+    lib.gpx_explorer_get_por_log.argtypes = [vp, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]
+    lib.gpx_train_options_init.argtypes = [C.POINTER(TrainOptions)]
+    lib.gpx_train_options_init.restype = None
+    lib.gpx_por_train.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(TrainOptions), C.POINTER(PorModel),
+                                  C.POINTER(C.c_float)]
+    fp = C.POINTER(C.c_float)
+    lib.gpx_por_grad.argtypes = [i, fp, fp, fp, C.c_float, C.c_void_p, fp, C.c_uint32, fp, fp, fp, fp, fp]
     lib.gpx_batch_options_init.argtypes = [C.POINTER(BatchOptions)]
     lib.gpx_batch_options_init.restype = None
     lib.gpx_batch_job_init.argtypes = [C.POINTER(BatchJob)]
@@ -262,6 +305,29 @@ class Explorer:
             raise GpxError(rc, "replacing model")
         self.model = model
 
+    def set_por_model(self, model: Optional["PorModel"]) -> None:
+        rc = load().gpx_explorer_set_por_model(self.handle, C.byref(model) if model is not None else None)
+        if rc != GPX_OK:
+            raise GpxError(rc, "setting the POR model")
+
+    def set_por_log(self, capacity: int, sample_every: int) -> None:
+        rc = load().gpx_explorer_set_por_log(self.handle, capacity, sample_every)
+        if rc != GPX_OK:
+            raise GpxError(rc, "setting the POR log")
+
+    def get_por_log(self) -> np.ndarray:
+        L = load()
+        n = C.c_uint64()
+        rc = L.gpx_explorer_get_por_log(self.handle, None, 0, C.byref(n))
+        if rc != GPX_OK:
+            raise GpxError(rc, "reading the POR log")
+        out = np.zeros(n.value, dtype=POR_LOG_DTYPE)
+        if n.value:
+            rc = L.gpx_explorer_get_por_log(self.handle, out.ctypes.data, n.value, C.byref(n))
+            if rc != GPX_OK:
+                raise GpxError(rc, "reading the POR log")
+        return out
+
     def dump(self, path: str) -> None:
         rc = load().gpx_explorer_dump(self.handle, path.encode())
         if rc != GPX_OK:
@@ -352,7 +418,12 @@ def batch_explore(models: Sequence[Model], jobs: Sequence[Dict], level_capacity:
             setattr(js[k], key, int(v))
     o = BatchOptions()
     lib.gpx_batch_options_init(C.byref(o))
+    keep = None
     for key, v in opts.items():
+        if key == "por_model":
+            keep = v
+            o.por_model = C.cast(C.pointer(v), C.c_void_p) if v is not None else None
+            continue
         setattr(o, key, float(v) if key == "load_factor" else int(v))
     items = (BatchItem * n)()
     levels = (C.c_uint64 * (n * level_capacity))()
@@ -371,7 +442,41 @@ def batch_explore(models: Sequence[Model], jobs: Sequence[Dict], level_capacity:
                     "completion_ms": it.completion_ms, "admissions": it.admissions})
     stats = {f: getattr(st, f) for f, _ in BatchStats._fields_}
     stats["rc"] = rc
+    del keep
     return out, stats
+
+
+def por_train(x: np.ndarray, y: np.ndarray, **kw):
+    """gpx_por_train: returns (PorModel, final loss)."""
+    L = load()
+    x = np.ascontiguousarray(x, dtype=np.uint8)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    o = TrainOptions()
+    L.gpx_train_options_init(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, float(v) if k in ("lr", "weight_decay") else int(v))
+    m = PorModel()
+    loss = C.c_float()
+    rc = L.gpx_por_train(x.ctypes.data, y.ctypes.data, x.shape[0], C.byref(o), C.byref(m), C.byref(loss))
+    if rc != GPX_OK:
+        raise GpxError(rc, "training the POR model")
+    return m, float(loss.value)
+
+
+def por_grad(w1, b1, w2, b2, x, y, device: int = 0):
+    """gpx_por_grad: (loss, gw1, gb1, gw2, gb2) of one forward/backward pass."""
+    L = load()
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32)  # noqa: E731
+    w1, b1, w2, y = f(w1), f(b1), f(w2), f(y)
+    x = np.ascontiguousarray(x, dtype=np.uint8)
+    gw1, gb1, gw2 = np.zeros_like(w1), np.zeros_like(b1), np.zeros_like(w2)
+    gb2, loss = C.c_float(), C.c_float()
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+    rc = L.gpx_por_grad(device, fp(w1), fp(b1), fp(w2), float(b2), x.ctypes.data, fp(y), x.shape[0], fp(gw1),
+                        fp(gb1), fp(gw2), C.byref(gb2), C.byref(loss))
+    if rc != GPX_OK:
+        raise GpxError(rc, "POR gradient")
+    return float(loss.value), gw1, gb1, gw2, float(gb2.value)
 
 
 def device_info(device: int = 0) -> Optional[DeviceInfo]:

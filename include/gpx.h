@@ -63,7 +63,7 @@ typedef struct {
     int32_t kernel_iters;   /* -k: BFS levels per kernel launch (0 = run to the end in one launch) */
     int32_t verbosity;      /* -v 0..3 (clamped to 3, GPUexplore.cu:1846-1848) */
     uint64_t q_words;       /* -q: hash-table size in 32-bit words (0 = half the free device memory) */
-    int32_t por;            /* --por: cluster-based ample-set reduction */
+    int32_t por;            /* --por: cluster-based ample-set reduction (2: with the learned proposal) */
     int32_t cycle_proviso;  /* --cycle-proviso */
     int32_t property;       /* gpx_property */
     int32_t device;         /* CUDA device ordinal */
@@ -196,6 +196,72 @@ int gpx_random_gather_probe(int device, uint64_t bytes, double *gathers_per_s);
 int gpx_explore_noalloc(const gpx_model *model, const gpx_options *opts, uint64_t *level_counts,
                         uint32_t level_capacity, gpx_result *result);
 
+/* ---- Learned cluster proposal for POR (no reference counterpart).
+ *
+ * With gpx_options.por == 2 (and a model set), the cluster each state expands is
+ * the valid cluster closure with the lowest score of a 2-layer MLP over
+ * GPX_POR_FEATURES small-integer features of the closure (its size, local
+ * targets and successors of its members, their synchronisation degree, members
+ * whose proviso holds, the process count, rules led, and the members' (process,
+ * local state) pairs hashed into 32 counts).  Layer 1: int8 weights times the
+ * integer features, summed exactly, then fp32 (acc * s1 + b1), ReLU, rounded to
+ * bf16; layer 2: int8 weights times the bf16 activations, fp32 FMA in order,
+ * then (acc * s2 + b2).  The proposal is re-checked -- non-empty, closed under
+ * the per-process clusters, some member's proviso holds -- and plain cample's
+ * choice is used when the check fails, so the reduction stays sound. */
+#define GPX_POR_FEATURES 40
+#define GPX_POR_HIDDEN 64
+typedef struct {
+    int8_t w1[GPX_POR_HIDDEN][GPX_POR_FEATURES];
+    float s1[GPX_POR_HIDDEN];
+    float b1[GPX_POR_HIDDEN];
+    int8_t w2[GPX_POR_HIDDEN];
+    float s2, b2;
+} gpx_por_model;
+
+/* One logged candidate of a state expanded with POR and the cycle proviso: its
+ * features, the successors its members generate, how many of them were not yet
+ * visited (the outcome used as training label), and plain cample's choice. */
+typedef struct {
+    uint8_t x[GPX_POR_FEATURES];
+    uint32_t succ;
+    uint32_t new_succ;
+    uint32_t state_tag;      /* hash of the source state: rows of one state share it */
+    uint8_t popc;
+    uint8_t cample_choice;   /* 1 if plain cample picks this closure */
+    uint8_t pad[2];
+} gpx_por_log_row;
+
+/* Use `model` for por == 2 (NULL: plain cample).  The model is copied. */
+int gpx_explorer_set_por_model(gpx_explorer *ex, const gpx_por_model *model);
+/* Log up to `capacity` candidate rows of states whose hash is 0 mod sample_every
+ * during the decide pass of later runs (por with the cycle proviso); 0 turns
+ * logging off.  gpx_explorer_get_por_log copies the rows of the last run. */
+int gpx_explorer_set_por_log(gpx_explorer *ex, uint64_t capacity, uint32_t sample_every);
+int gpx_explorer_get_por_log(gpx_explorer *ex, gpx_por_log_row *rows, uint64_t capacity, uint64_t *nrows);
+
+/* Training of the proposal MLP on the GPU with this library's forward and
+ * backward kernels (fp32 master weights, int8 fake-quantised weights and bf16
+ * activations in the forward pass, straight-through gradients, Adam, mean
+ * squared error), exported as a gpx_por_model. */
+typedef struct {
+    uint32_t struct_size;
+    int32_t device;
+    uint32_t epochs;
+    uint32_t batch;
+    float lr;
+    float weight_decay;
+    uint64_t seed;
+} gpx_train_options;
+void gpx_train_options_init(gpx_train_options *o);
+int gpx_por_train(const uint8_t *x, const float *y, uint64_t rows, const gpx_train_options *o,
+                  gpx_por_model *out, float *final_loss);
+/* One forward and backward pass over `rows` rows with the given fp32 weights
+ * (w1 [H][F], b1 [H], w2 [H], b2), as the training kernels compute them:
+ * mean-squared-error loss and its gradients (for checking them). */
+int gpx_por_grad(int device, const float *w1, const float *b1, const float *w2, float b2, const uint8_t *x,
+                 const float *y, uint32_t rows, float *gw1, float *gb1, float *gw2, float *gb2, float *loss);
+
 /* ---- Batched exploration (no reference counterpart: the reference explores one
  * network per process).  Many networks of uneven size explored in one
  * persistent launch; each has its own hash-table and state-store partition,
@@ -206,7 +272,7 @@ int gpx_explore_noalloc(const gpx_model *model, const gpx_options *opts, uint64_
 typedef struct {
     uint32_t struct_size;
     int32_t property;       /* gpx_property */
-    int32_t por;            /* 0: none, 1: cluster POR */
+    int32_t por;            /* 0: none, 1: cluster POR, 2: cluster POR with the learned proposal */
     int32_t cycle_proviso;
     uint64_t max_states;    /* state budget (0 = none) */
     uint64_t capacity;      /* states admitted (table + store partition); 0 = estimate */
@@ -236,6 +302,7 @@ typedef struct {
     int32_t max_admissions; /* launches per instance before an overflow is final (0 = 3) */
     double load_factor;     /* table slots = admitted states / load_factor (0 = 0.5) */
     uint64_t seed;
+    const gpx_por_model *por_model; /* for jobs with por == 2 (NULL: plain cample) */
 } gpx_batch_options;
 
 typedef struct {

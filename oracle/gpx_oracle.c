@@ -42,6 +42,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <math.h>
 #include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
@@ -263,6 +264,9 @@ typedef struct {
 
 typedef void (*emit_fn)(void *ctx, const uint32_t *succ, origin_t o);
 
+/* When set (per thread), counts each applicable rule at its lowest member. */
+static __thread uint32_t *g_rules_led = NULL;
+
 /* Enumerate every successor of v (G:904-949 local, G:954-1122 synchronising). */
 static int expand_all(const gpf_t *m, const uint32_t *v, const expand_t *x, emit_fn emit, void *ctx) {
     uint32_t succ[16];
@@ -299,6 +303,7 @@ static int expand_all(const gpf_t *m, const uint32_t *v, const expand_t *x, emit
                     uint32_t rule = (m->syncbits[w] >> (f * n)) & ((n == 32) ? 0xFFFFFFFFu : ((1u << n) - 1u));
                     if (!rule || (rule & en) != rule) continue; /* G:1016, G:1488 */
                     enabled = 1;
+                    if (g_rules_led) g_rules_led[__builtin_ctz(rule)]++;
                     /* Cartesian product over the participants' a-targets (G:1030-1119) */
                     const actset_t *g[MAXP];
                     uint32_t parts[MAXP], np = 0, idx[MAXP];
@@ -325,6 +330,60 @@ static int expand_all(const gpf_t *m, const uint32_t *v, const expand_t *x, emit
     return enabled;
 }
 
+/* ------------------------------------------------- learned cluster proposal */
+
+/* The proposal MLP in the byte layout of gpx_por_model (include/gpx.h): int8
+ * w1[64][40], float s1[64], float b1[64], int8 w2[64], float s2, b2.  The
+ * selection below restates the GPU's exactly: integer features, an exact integer
+ * layer-1 sum, fmaf in the same order, bfloat16 round-to-nearest-even. */
+#define PF 40
+#define PH 64
+typedef struct {
+    int8_t w1[PH][PF];
+    float s1[PH];
+    float b1[PH];
+    int8_t w2[PH];
+    float s2, b2;
+} por_model_t;
+
+static por_model_t *g_por_model = NULL;
+
+static float bf16_round(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    u &= 0xFFFF0000u;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+static uint32_t por_hash_bucket(uint32_t p, uint32_t s) {
+    uint32_t h = (p * 0x9E3779B1u) ^ (s * 0x85EBCA77u);
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    return h >> 27;
+}
+
+static float por_score(const por_model_t *m, const uint32_t *x) {
+    float out = 0.0f;
+    for (int k = 0; k < PH; k++) {
+        int acc = 0;
+        for (int j = 0; j < PF; j++) acc += (int)m->w1[k][j] * (int)x[j];
+        float h = fmaf((float)acc, m->s1[k], m->b1[k]);
+        h = h > 0.0f ? h : 0.0f;
+        h = bf16_round(h);
+        out = fmaf((float)m->w2[k], h, out);
+    }
+    return fmaf(out, m->s2, m->b2);
+}
+
+static uint32_t float_key(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
 /* Static cluster of process p: {p} plus every rule containing p of an action
  * that p has enabled, whether or not the rule is applicable (G:1616-1624). */
 static uint32_t static_cluster(const gpf_t *m, const expand_t *x, uint32_t p) {
@@ -346,11 +405,20 @@ static uint32_t static_cluster(const gpf_t *m, const expand_t *x, uint32_t p) {
  * cluster relation, keep closures with at least one member whose proviso held,
  * take the one with the fewest processes (ties: lowest process index); default
  * is every process (full expansion). */
-static uint32_t select_cluster(uint32_t n, const uint32_t *cl, uint32_t prov) {
+typedef struct {
+    uint32_t succ[MAXP];   /* successors each process leads (local targets + led rules' products) */
+    uint32_t nlocal[MAXP]; /* local targets */
+    uint32_t rules[MAXP];  /* applicable rules led */
+    uint32_t s[MAXP];      /* local states */
+} por_ctx_t;
+
+static uint32_t select_cluster(uint32_t n, const uint32_t *cl, uint32_t prov, const por_ctx_t *pc) {
     uint32_t c[MAXP];
     for (uint32_t p = 0; p < n; p++) c[p] = (prov >> p & 1u) ? cl[p] : (cl[p] & ~(1u << p));
     uint32_t best = (n == 32) ? 0xFFFFFFFFu : ((1u << n) - 1u);
     uint32_t bestc = n;
+    uint64_t lbest = ~0ull;
+    uint32_t lsel = 0;
     for (uint32_t p = 0; p < n; p++) {
         uint32_t closure = c[p], todo = c[p], valid = 0;
         while (todo) {
@@ -364,6 +432,43 @@ static uint32_t select_cluster(uint32_t n, const uint32_t *cl, uint32_t prov) {
             bestc = (uint32_t)__builtin_popcount(closure);
             best = closure;
         }
+        if (g_por_model && pc && valid && closure) {
+            /* features of the candidate (the GPU's cluster_features) */
+            uint32_t x[PF];
+            memset(x, 0, sizeof x);
+            uint32_t lt = 0, sc = 0, deg = 0, rl = 0;
+            for (uint32_t q = 0; q < n; q++)
+                if (closure >> q & 1u) {
+                    lt += pc->nlocal[q];
+                    sc += pc->succ[q];
+                    deg += (uint32_t)__builtin_popcount(cl[q]);
+                    rl += pc->rules[q];
+                    x[8 + por_hash_bucket(q, pc->s[q])]++;
+                }
+            x[0] = (uint32_t)__builtin_popcount(closure);
+            x[1] = lt < 255 ? lt : 255;
+            x[2] = sc < 255 ? sc : 255;
+            x[3] = deg < 255 ? deg : 255;
+            x[4] = (uint32_t)__builtin_popcount(closure & prov);
+            x[5] = n;
+            x[6] = rl < 255 ? rl : 255;
+            x[7] = 1;
+            float sco = por_score(g_por_model, x);
+            if (isfinite(sco)) {
+                uint64_t key = ((uint64_t)float_key(sco) << 32) | (((uint32_t)__builtin_popcount(closure) << 5) | p);
+                if (key < lbest) {
+                    lbest = key;
+                    lsel = closure;
+                }
+            }
+        }
+    }
+    if (lbest != ~0ull) {
+        /* re-check the proposal: non-empty, closed, a member whose proviso holds */
+        int closed = lsel != 0, some = (lsel & prov) != 0;
+        for (uint32_t q = 0; q < n; q++)
+            if ((lsel >> q & 1u) && (c[q] & ~lsel)) closed = 0;
+        if (closed && some) return lsel;
     }
     return best;
 }
@@ -475,6 +580,7 @@ typedef struct {
     vec_t *out; /* [nshards] for the calling thread */
     uint32_t sel;
     uint64_t generated;
+    por_ctx_t pc; /* per-process facts for the learned proposal */
 } sctx_t;
 
 static inline uint32_t shard_of(uint64_t h, uint32_t nshards) {
@@ -496,6 +602,7 @@ static void emit_decide(void *ctx, const uint32_t *succ, origin_t o) {
         sat = !hset_find(&c->shards[shard_of(h, c->nshards)], succ, h);
     }
     if (sat) c->prov |= o.mask; /* local: bit p; synchronisation: every member (G:1616-1624) */
+    c->pc.succ[__builtin_ctz(o.mask)]++;    /* attributed to the lowest member, as the GPU's leader */
 }
 
 /* Pass-2 sink: keep successors of transitions inside the selected cluster
@@ -540,12 +647,19 @@ static uint32_t decide(sctx_t *c, const uint32_t *v, expand_t *x, int *deadlock)
     const gpf_t *m = c->m;
     collect(m, v, x);
     c->prov = 0;
+    memset(&c->pc, 0, sizeof c->pc);
+    g_rules_led = c->pc.rules;
     int enabled = expand_all(m, v, x, emit_decide, c);
+    g_rules_led = NULL;
     if (!enabled) *deadlock = 1;
     if (!c->o->por) return 0xFFFFFFFFu;
     uint32_t cl[MAXP];
-    for (uint32_t p = 0; p < m->nr_procs; p++) cl[p] = static_cluster(m, x, p);
-    return select_cluster(m->nr_procs, cl, c->prov);
+    for (uint32_t p = 0; p < m->nr_procs; p++) {
+        cl[p] = static_cluster(m, x, p);
+        c->pc.nlocal[p] = x->nlocal[p];
+        c->pc.s[p] = get_local(m, v, p);
+    }
+    return select_cluster(m->nr_procs, cl, c->prov, c->o->por == 2 ? &c->pc : NULL);
 }
 
 static int run(const gpf_t *m, const opts_t *o, result_t *res) {
@@ -721,8 +835,17 @@ int main(int argc, char **argv) {
         } else if (!strcmp(argv[i], "-p")) {
             o.property = PROP_SAFETY;
             o.proviso = 1;
+        } else if (!strcmp(argv[i], "--por-model") && i + 1 < argc) {
+            FILE *pf = fopen(argv[++i], "rb");
+            g_por_model = (por_model_t *)calloc(1, sizeof(por_model_t));
+            if (!pf || fread(g_por_model, sizeof(por_model_t), 1, pf) != 1) {
+                fprintf(stderr, "ERROR: cannot read POR model %s\n", argv[i]);
+                return 1;
+            }
+            fclose(pf);
+            o.por = 2;
         } else if (!strcmp(argv[i], "--por")) {
-            o.por = 1;
+            if (!o.por) o.por = 1;
         } else if (!strcmp(argv[i], "--cycle-proviso")) {
             if (o.property == PROP_NONE) o.proviso = 1;
         } else if (!strcmp(argv[i], "--threads") && i + 1 < argc) {
