@@ -230,9 +230,21 @@ def run_other_workload(args, local):
                 ms += r["setup_ms"] + r["kernel_ms"]
                 kms += r["kernel_ms"]
                 states += r["states"]
+        extra = {}
+        if args.workload == "config1":
+            # the same ten rings in one batched launch (gpx_batch_explore)
+            jobs = [{"property": "deadlock", "capacity": 1 << 18} for _ in nets]
+            for _ in range(args.warmup):
+                lib.batch_explore(models, jobs)
+            bms, bst = 0.0, 0
+            for _ in range(args.steps):
+                items, st = lib.batch_explore(models, jobs)
+                bms += st["device_ms"]
+                bst += st["states"]
+            extra = {"batched_states_per_s": bst / (bms / 1000.0), "batched_ms_per_step": bms / args.steps}
         line.update(value=states / (ms / 1000.0), ms_per_step=ms / args.steps,
                     config={"workload": desc, "states_per_step": states // args.steps, "networks": len(nets),
-                            "kernel_ms_per_step": kms / args.steps})
+                            "kernel_ms_per_step": kms / args.steps, **extra})
     else:
         rng = random.Random(5)
         nets = gen.batch(5, count=args.batch_count)

@@ -91,8 +91,10 @@ template <int MODE> __device__ void close_phase(const Params &P) {
     c->hi = newhi;
     c->cursor = 0;
     c->phase = (MODE == MODE_PROVISO) ? PH_DECIDE : PH_EXPAND;
+    // claims shrink with the level (down to one state) so that small levels
+    // spread over every warp instead of queueing behind a few long batches
     unsigned long long per = cnt / ((unsigned long long)P.total_warps * 4ull);
-    c->claim = (unsigned int)(per < 32 ? 32 : (per > 4096 ? 4096 : per));
+    c->claim = (unsigned int)(per < 1 ? 1 : (per > 4096 ? 4096 : per));
     if (P.levels_per_launch && c->launch_levels >= P.levels_per_launch && !c->done) c->pause = 1;
 }
 
@@ -137,12 +139,13 @@ template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_k
     Explorer<K, MODE> E(P, model, ws);
     Ctrl *c = P.ctrl;
     const uint32_t n = E.M.n;
-    uint32_t B = kPairMax / n;
-    if (B > 32) B = 32;
-    if (B < 1) B = 1;
+    uint32_t Bmax = kPairMax / n;
+    if (Bmax > 32) Bmax = 32;
+    if (Bmax < 1) Bmax = 1;
     for (;;) {
         unsigned long long lo = vload(&c->lo), hi = vload(&c->hi);
         unsigned int claim = vload(&c->claim);
+        const uint32_t B = claim < Bmax ? claim : Bmax;
         bool decide = (MODE == MODE_PROVISO) && vload(&c->phase) == PH_DECIDE;
         unsigned long long nlev = hi - lo;
         for (;;) {
@@ -620,7 +623,7 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     c0.lo = 0;
     c0.hi = 1;
     c0.nlevels = 1;
-    c0.claim = 32;
+    c0.claim = 1;
     c0.phase = ex->mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND;
     *ex->h_ctrl = c0;
     GPX_CUDA(cudaMemcpyAsync(ex->d_ctrl, ex->h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, ex->st));
@@ -1061,7 +1064,7 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     c.store_count = 1;
     c.hi = 1;
     c.nlevels = 1;
-    c.claim = 32;
+    c.claim = 1;
     c.phase = mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND;
     GPX_CUDA(cudaMemcpyAsync(base + off_model, model->dec.words.data(), model_bytes, cudaMemcpyHostToDevice, st));
     GPX_CUDA(cudaMemsetAsync(P.table, 0, tb, st));
