@@ -140,7 +140,8 @@ static __device__ void close_instance(const BParams &BP, BInst *I, unsigned int 
 
 template <int MODE>
 static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char *raw, unsigned long long lo,
-                                     unsigned long long off, unsigned long long cnt, bool decide) {
+                                     unsigned long long off, unsigned long long cnt, unsigned long long claim,
+                                     bool decide) {
     Params P;
     memset(&P, 0, sizeof P);
     P.table = I->table;
@@ -157,6 +158,7 @@ static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char 
     Explorer<K128, MODE> E(P, I->model, *(WarpScratch<K128, MODE> *)raw);
     uint32_t B = kPairMax / E.M.n;
     B = B > 32 ? 32 : (B < 1 ? 1 : B);
+    if (B > claim) B = (uint32_t)claim; // small claims: one batch per claim, spread over warps
     for (unsigned long long b = off; b < off + cnt; b += B) {
         uint32_t n = (uint32_t)((off + cnt - b) < B ? (off + cnt - b) : B);
         E.batch(lo + b, n, b, decide);
@@ -164,7 +166,7 @@ static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char 
     E.flush_stats(); // appends the staged new states before the chunk is reported
 }
 
-__global__ void __launch_bounds__(256, 4) batch_kernel(BParams BP) {
+__global__ void __launch_bounds__(256, 3) batch_kernel(BParams BP) {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned char *raw = smem + (size_t)(threadIdx.x >> 5) * sizeof(WarpScratch<K128, MODE_PROVISO>);
     const uint32_t lane = threadIdx.x & 31;
@@ -187,6 +189,7 @@ __global__ void __launch_bounds__(256, 4) batch_kernel(BParams BP) {
             BLevel L = read_level(I, e);
             unsigned long long n = L.hi - L.lo;
             if ((t & kCurMask) >= n) continue;
+            // level-sized claims (at least the tuned size) keep few-state levels on many warps
             unsigned long long claim = n / ((unsigned long long)BP.total_warps * 4ull);
             claim = claim < BP.claim ? BP.claim : (claim > 4096 ? 4096 : claim);
             unsigned long long old = 0;
@@ -203,11 +206,11 @@ __global__ void __launch_bounds__(256, 4) batch_kernel(BParams BP) {
             unsigned long long cnt = (n - cur) < claim ? (n - cur) : claim;
             bool decide = L.phase == PH_DECIDE;
             if (I->mode == MODE_PLAIN)
-                process_claim<MODE_PLAIN>(BP, I, raw, L.lo, cur, cnt, false);
+                process_claim<MODE_PLAIN>(BP, I, raw, L.lo, cur, cnt, claim, false);
             else if (I->mode == MODE_POR)
-                process_claim<MODE_POR>(BP, I, raw, L.lo, cur, cnt, false);
+                process_claim<MODE_POR>(BP, I, raw, L.lo, cur, cnt, claim, false);
             else
-                process_claim<MODE_PROVISO>(BP, I, raw, L.lo, cur, cnt, decide);
+                process_claim<MODE_PROVISO>(BP, I, raw, L.lo, cur, cnt, claim, decide);
             __threadfence();
             if (lane == 0) {
                 unsigned long long d = atomicAdd(&I->completed[e2 & 1], cnt) + cnt;
@@ -559,7 +562,7 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
         double best = 1e30;
         BatchConfig bestc = cfg;
         for (int threads : {128, 256})
-            for (int claim : {32, 64, 128, 256})
+            for (int claim : {8, 32, 64, 256})
                 for (double lf : {0.25, 0.5}) {
                     BatchConfig c = cfg;
                     c.threads = threads;
