@@ -311,28 +311,48 @@ struct WarpStats {
     unsigned int violation;
 };
 
-// Model accessors over the device layout (gpx_model.h).
+// Model accessors over the device layout (gpx_model.h).  The array bases are
+// resolved once; a process's bit field and record base come from one packed word.
 struct MView {
     const uint32_t *w;
     uint32_t n;
-    __device__ uint32_t fb(uint32_t p) const { return w[H_FB + p]; }
-    __device__ uint32_t bs(uint32_t p) const { return w[H_BS + p]; }
-    __device__ const uint32_t *rec(uint32_t p, uint32_t s) const {
-        return w + w[H_OFF_RECS] + (w[H_PSBASE + p] + s) * kRecWords;
+    const uint32_t *recs, *ltgt_, *sent_, *stgt_, *rules_, *lrule_;
+    __device__ void init(const uint32_t *m) {
+        w = m;
+        n = m[H_NPROCS];
+        recs = m + m[H_OFF_RECS];
+        ltgt_ = m + m[H_OFF_LTGT];
+        sent_ = m + m[H_OFF_SENT];
+        stgt_ = m + m[H_OFF_STGT];
+        rules_ = m + m[H_OFF_RULES];
+        lrule_ = m + m[H_OFF_LRULE];
     }
-    __device__ uint32_t ltgt(uint32_t i) const { return w[w[H_OFF_LTGT] + i]; }
-    __device__ uint32_t stgt(uint32_t i) const { return w[w[H_OFF_STGT] + i]; }
-    __device__ uint32_t lrule(uint32_t i) const { return w[w[H_OFF_LRULE] + i]; }
-    __device__ uint32_t rmask(uint32_t k) const { return w[w[H_OFF_RULES] + 2 * k]; }
-    __device__ uint32_t ract(uint32_t k) const { return w[w[H_OFF_RULES] + 2 * k + 1]; }
+    __device__ uint32_t pd(uint32_t p) const { return w[H_PDESC + p]; }
+    static __device__ uint32_t fb_of(uint32_t d) { return d & 127u; }
+    static __device__ uint32_t bs_of(uint32_t d) { return (d >> 7) & 31u; }
+    __device__ const uint32_t *rec_of(uint32_t d, uint32_t s) const { return recs + ((d >> 12) + s) * kRecWords; }
+    __device__ uint32_t fb(uint32_t p) const { return fb_of(pd(p)); }
+    __device__ uint32_t bs(uint32_t p) const { return bs_of(pd(p)); }
+    __device__ const uint32_t *rec(uint32_t p, uint32_t s) const { return rec_of(pd(p), s); }
+    __device__ uint32_t ltgt(uint32_t i) const { return ltgt_[i]; }
+    __device__ uint32_t stgt(uint32_t i) const { return stgt_[i]; }
+    __device__ uint32_t lrule(uint32_t i) const { return lrule_[i]; }
+    __device__ uint32_t rmask(uint32_t k) const { return rules_[2 * k]; }
+    __device__ uint32_t ract(uint32_t k) const { return rules_[2 * k + 1]; }
     // synchronising group of (p, s) for action a: {action, toff, tcnt, has1} or null
     __device__ const uint32_t *group(const uint32_t *rec, uint32_t a) const {
-        const uint32_t *g = w + w[H_OFF_SENT] + rec[R_SOFF] * 4;
+        const uint32_t *g = sent_ + rec[R_SOFF] * 4;
         for (uint32_t i = 0; i < rec[R_SCNT]; i++, g += 4) {
             if (g[0] == a) return g;
             if (g[0] > a) break;
         }
         return nullptr;
+    }
+    // local state of process p in `key` and its record
+    template <class K> __device__ const uint32_t *state_rec(const K &key, uint32_t p, uint32_t &s) const {
+        uint32_t d = pd(p);
+        s = KT<K>::get(key, fb_of(d), bs_of(d));
+        return rec_of(d, s);
     }
 };
 
@@ -422,8 +442,7 @@ template <class K, int MODE> struct Explorer {
 
     __device__ Explorer(const Params &p, const uint32_t *model, WarpScratch<K, MODE> &w)
         : P(p), ws(w), table((K *)p.table), store((K *)p.store) {
-        M.w = model;
-        M.n = model[H_NPROCS];
+        M.init(model);
         lane = threadIdx.x & 31;
         lanemask_lt = (1u << lane) - 1u;
         shead = scount = 0;
@@ -438,7 +457,8 @@ template <class K, int MODE> struct Explorer {
         while (rest) {
             uint32_t q = __ffs(rest) - 1;
             rest &= rest - 1;
-            psz *= M.group(M.rec(q, KT<K>::get(key, M.fb(q), M.bs(q))), act)[2];
+            uint32_t sq;
+            psz *= M.group(M.state_rec(key, q, sq), act)[2];
         }
         return psz;
     }
@@ -484,8 +504,8 @@ template <class K, int MODE> struct Explorer {
         for (uint32_t i = lane; i < npairs; i += 32) {
             uint32_t g = i / n, p = i - g * n;
             K key = ws.keys[g];
-            uint32_t s = KT<K>::get(key, M.fb(p), M.bs(p));
-            const uint32_t *rec = M.rec(p, s);
+            uint32_t s;
+            const uint32_t *rec = M.state_rec(key, p, s);
             uint32_t lcnt = rec[R_LCNT], roff = rec[R_ROFF], rcnt = rec[R_RCNT];
             uint32_t appl = 0, provbits = lcnt ? (1u << p) : 0u, cnt = lcnt;
             bool viol = safety && check && p == n - 1 && (rec[R_FLAGS] & 1u);
@@ -497,8 +517,8 @@ template <class K, int MODE> struct Explorer {
                 while (rest) {
                     uint32_t q = __ffs(rest) - 1;
                     rest &= rest - 1;
-                    uint32_t sq = (q == p) ? s : KT<K>::get(key, M.fb(q), M.bs(q));
-                    const uint32_t *grp = M.group(q == p ? rec : M.rec(q, sq), act);
+                    uint32_t sq;
+                    const uint32_t *grp = M.group(q == p ? rec : M.state_rec(key, q, sq), act);
                     if (!grp) {
                         ok = false;
                         break;
@@ -540,7 +560,8 @@ template <class K, int MODE> struct Explorer {
                 uint32_t g = i / n, p = i - g * n;
                 uint32_t sel = ws.sel[g];
                 K key = ws.keys[g];
-                const uint32_t *rec = M.rec(p, KT<K>::get(key, M.fb(p), M.bs(p)));
+                uint32_t sp;
+                const uint32_t *rec = M.state_rec(key, p, sp);
                 uint32_t cnt = (sel >> p & 1u) ? rec[R_LCNT] : 0u;
                 uint32_t a = ws.appl[i], keep = 0, roff = rec[R_ROFF];
                 while (a) {
@@ -590,11 +611,12 @@ template <class K, int MODE> struct Explorer {
                 og = lo / n;
                 uint32_t p = lo - og * n;
                 K key = ws.keys[og];
-                const uint32_t *rec = M.rec(p, KT<K>::get(key, M.fb(p), M.bs(p)));
+                const uint32_t dp = M.pd(p);
+                const uint32_t *rec = M.rec_of(dp, KT<K>::get(key, MView::fb_of(dp), MView::bs_of(dp)));
                 uint32_t lcnt = (!filter || (ws.sel[og] >> p & 1u)) ? rec[R_LCNT] : 0u;
                 out = key;
                 if (sub < lcnt) {
-                    KT<K>::set(out, M.fb(p), M.bs(p), M.ltgt(rec[R_LOFF] + sub));
+                    KT<K>::set(out, MView::fb_of(dp), MView::bs_of(dp), M.ltgt(rec[R_LOFF] + sub));
                     omask = 1u << p;
                 } else {
                     sub -= lcnt;
@@ -612,10 +634,12 @@ template <class K, int MODE> struct Explorer {
                         while (rest) {
                             uint32_t q = __ffs(rest) - 1;
                             rest &= rest - 1;
-                            const uint32_t *grp = M.group(M.rec(q, KT<K>::get(key, M.fb(q), M.bs(q))), act);
+                            const uint32_t dq = M.pd(q);
+                            const uint32_t *grp =
+                                M.group(M.rec_of(dq, KT<K>::get(key, MView::fb_of(dq), MView::bs_of(dq))), act);
                             uint32_t tc = grp[2], d = sub % tc;
                             sub /= tc;
-                            KT<K>::set(out, M.fb(q), M.bs(q), M.stgt(grp[1] + d));
+                            KT<K>::set(out, MView::fb_of(dq), MView::bs_of(dq), M.stgt(grp[1] + d));
                         }
                         omask = mask;
                         break;

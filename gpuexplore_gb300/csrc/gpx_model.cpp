@@ -238,6 +238,7 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
     }
     psbase[n] = (uint32_t)(recs.size() / kRecWords);
     if (max_lrules > 32) return "UNSUPPORTED: a process leads more than 32 rules in one local state";
+    if (psbase[n] >= (1u << 20)) return "UNSUPPORTED: more than 2^20 (process, local state) records";
 
     std::vector<uint32_t> &wds = out->words;
     wds.assign(kHdrWords, 0);
@@ -246,6 +247,7 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
     for (uint32_t p = 0; p <= n; p++) wds[H_FB + p] = g.firstbit[p];
     for (uint32_t p = 0; p < n; p++) wds[H_BS + p] = g.bits_state[p];
     for (uint32_t p = 0; p <= n; p++) wds[H_PSBASE + p] = psbase[p];
+    for (uint32_t p = 0; p < n; p++) wds[H_PDESC + p] = g.firstbit[p] | (g.bits_state[p] << 7) | (psbase[p] << 12);
     auto append = [&](const std::vector<uint32_t> &v) {
         uint32_t off = (uint32_t)wds.size();
         wds.insert(wds.end(), v.begin(), v.end());

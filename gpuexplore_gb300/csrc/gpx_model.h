@@ -16,7 +16,7 @@ namespace gpx {
 
 constexpr int kMaxProcs = 31;      // rule masks are nr_procs bits (GPUexplore.cu:980, 995)
 constexpr int kMaxStateBits = 126; // widest state vector a 128-bit slot holds (63 + 63 bits)
-constexpr int kHdrWords = 128;     // words of the device-layout header
+constexpr int kHdrWords = 160;     // words of the device-layout header
 constexpr int kRecWords = 8;       // words per (process, local state) record
 
 // Raw gpf fields, named as in the reference.
@@ -49,6 +49,7 @@ enum HdrIndex : int {
     H_NRULES = 106,
     H_TOTAL_WORDS = 107,
     H_MAX_LRULES = 108, // most rules led by one (process, state)
+    H_PDESC = 128,      // per process: firstbit | bits_state << 7 | record base << 12 (32 words)
 };
 
 // Record fields (kRecWords words per (p, s)).
