@@ -480,6 +480,57 @@ template <class K, int MODE> struct Explorer {
         __syncwarp();
     }
 
+    // Successor number t of the batch (ws.pre holds the per-pair prefix): the
+    // pair's local targets first, then the products of the rules it leads.
+    __device__ void materialise(uint32_t t, uint32_t npairs, bool filter, K &out, uint32_t &og,
+                                uint32_t &omask) const {
+        const uint32_t n = M.n;
+        uint32_t lo = 0, hi = npairs;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (ws.pre[mid] <= t) lo = mid;
+            else hi = mid;
+        }
+        uint32_t sub = t - ws.pre[lo];
+        og = lo / n;
+        uint32_t p = lo - og * n;
+        K key = ws.keys[og];
+        const uint32_t dp = M.pd(p);
+        const uint32_t *rec = M.rec_of(dp, KT<K>::get(key, MView::fb_of(dp), MView::bs_of(dp)));
+        uint32_t lcnt = (!filter || (ws.sel[og] >> p & 1u)) ? rec[R_LCNT] : 0u;
+        out = key;
+        omask = 0;
+        if (sub < lcnt) {
+            KT<K>::set(out, MView::fb_of(dp), MView::bs_of(dp), M.ltgt(rec[R_LOFF] + sub));
+            omask = 1u << p;
+            return;
+        }
+        sub -= lcnt;
+        uint32_t a = ws.appl[lo], roff = rec[R_ROFF];
+        while (a) {
+            uint32_t r = __ffs(a) - 1;
+            a &= a - 1;
+            uint32_t k = M.lrule(roff + r), mask = M.rmask(k), act = M.ract(k);
+            uint32_t psz = product_size(key, mask, act);
+            if (sub >= psz) {
+                sub -= psz;
+                continue;
+            }
+            uint32_t rest = mask;
+            while (rest) {
+                uint32_t q = __ffs(rest) - 1;
+                rest &= rest - 1;
+                const uint32_t dq = M.pd(q);
+                const uint32_t *grp = M.group(M.rec_of(dq, KT<K>::get(key, MView::fb_of(dq), MView::bs_of(dq))), act);
+                uint32_t tc = grp[2], d = sub % tc;
+                sub /= tc;
+                KT<K>::set(out, MView::fb_of(dq), MView::bs_of(dq), M.stgt(grp[1] + d));
+            }
+            omask = mask;
+            return;
+        }
+    }
+
     // Expand a batch of B states store[first .. first+B).
     __device__ void batch(unsigned long long first, uint32_t B, unsigned long long lvl_off, bool decide) {
         const uint32_t n = M.n;
@@ -600,52 +651,7 @@ template <class K, int MODE> struct Explorer {
             bool valid = t < carry;
             K out;
             uint32_t og = 0, omask = 0;
-            if (valid) {
-                uint32_t lo = 0, hi = npairs;
-                while (hi - lo > 1) {
-                    uint32_t mid = (lo + hi) >> 1;
-                    if (ws.pre[mid] <= t) lo = mid;
-                    else hi = mid;
-                }
-                uint32_t sub = t - ws.pre[lo];
-                og = lo / n;
-                uint32_t p = lo - og * n;
-                K key = ws.keys[og];
-                const uint32_t dp = M.pd(p);
-                const uint32_t *rec = M.rec_of(dp, KT<K>::get(key, MView::fb_of(dp), MView::bs_of(dp)));
-                uint32_t lcnt = (!filter || (ws.sel[og] >> p & 1u)) ? rec[R_LCNT] : 0u;
-                out = key;
-                if (sub < lcnt) {
-                    KT<K>::set(out, MView::fb_of(dp), MView::bs_of(dp), M.ltgt(rec[R_LOFF] + sub));
-                    omask = 1u << p;
-                } else {
-                    sub -= lcnt;
-                    uint32_t a = ws.appl[lo], roff = rec[R_ROFF];
-                    while (a) {
-                        uint32_t r = __ffs(a) - 1;
-                        a &= a - 1;
-                        uint32_t k = M.lrule(roff + r), mask = M.rmask(k), act = M.ract(k);
-                        uint32_t psz = product_size(key, mask, act);
-                        if (sub >= psz) {
-                            sub -= psz;
-                            continue;
-                        }
-                        uint32_t rest = mask;
-                        while (rest) {
-                            uint32_t q = __ffs(rest) - 1;
-                            rest &= rest - 1;
-                            const uint32_t dq = M.pd(q);
-                            const uint32_t *grp =
-                                M.group(M.rec_of(dq, KT<K>::get(key, MView::fb_of(dq), MView::bs_of(dq))), act);
-                            uint32_t tc = grp[2], d = sub % tc;
-                            sub /= tc;
-                            KT<K>::set(out, MView::fb_of(dq), MView::bs_of(dq), M.stgt(grp[1] + d));
-                        }
-                        omask = mask;
-                        break;
-                    }
-                }
-            }
+            if (valid) materialise(t, npairs, filter, out, og, omask);
             if (MODE == MODE_PROVISO && decide) {
                 if (valid) {
                     st.lookups++;
