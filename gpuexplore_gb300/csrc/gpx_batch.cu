@@ -152,6 +152,7 @@ static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char 
     P.sel = I->sel;
     P.ctrl = &I->ctrl;
     P.seed = BP.seed;
+    P.timeout_ns = BP.timeout_ns;
     P.property = I->property;
     P.por_model = I->por_model;
     P.learned = I->por_model ? 1u : 0u;

@@ -42,6 +42,8 @@ struct Ctrl {
     unsigned int launch_levels;     // levels closed in this launch
     unsigned int bar_count, bar_gen;
     unsigned int timeout_at;        // where a bounded wait gave up (diagnostics)
+    unsigned long long overflow_count; // keys whose probe sequence was full during this level
+    unsigned long long evictions;      // keys displaced to make room
 };
 
 struct Params {
@@ -61,6 +63,9 @@ struct Params {
     uint32_t property;
     uint32_t levels_per_launch;
     uint32_t total_warps;
+    // keys whose probe sequence was full, placed by the closing thread
+    void *overflow;
+    unsigned long long overflow_cap;
     // learned cluster proposal (por == 2) and candidate logging (decide pass)
     const gpx_por_model *por_model;
     uint32_t learned;
@@ -233,9 +238,10 @@ static __device__ __forceinline__ unsigned long long bucket_of(uint64_t h, int i
 
 // Find-or-insert.  Returns 0 if the key was present, 1 if this call inserted
 // it, 2 if every probed bucket was full.  Slots go from empty to a key exactly
-// once; every caller scans the same probe sequence and claims the first empty
-// slot it sees with a full-key CAS, so two insertions of one key always meet in
-// the same slot and exactly one wins.
+// once during a level (keys move only in place_evicting, when no other thread
+// inserts); every caller scans the same probe sequence and claims the first
+// empty slot it sees with a full-key CAS, so two insertions of one key always
+// meet in the same slot and exactly one wins.
 template <class K>
 __device__ __forceinline__ int find_or_insert(K *table, unsigned long long nb, const K &key, uint64_t h,
                                               unsigned int &probes) {
@@ -260,6 +266,86 @@ __device__ __forceinline__ int find_or_insert(K *table, unsigned long long nb, c
         }
     }
     return 2;
+}
+
+// Bounded eviction, run by a single thread while no other thread touches the
+// table (at the end of a level): place a key whose probe sequence was full by
+// moving one occupant V of that sequence to the first empty slot further along
+// V's own sequence, then writing the key where V was.  Both sequences keep
+// "every slot before a key's position is occupied", so lookups stay exact.
+// Returns 0 (already present), 1 (placed), 2 (no displacement found).
+template <class K>
+__device__ int place_evicting(K *table, unsigned long long nb, const K &key, unsigned long long seed,
+                              unsigned long long &evictions) {
+    constexpr int S = KT<K>::kSlots;
+    const uint64_t h = KT<K>::hash(key, seed);
+    for (int i = 0; i < kMaxProbe; i++) { // placed meanwhile (a duplicate overflow entry) or room after all
+        K *b = table + bucket_of(h, i, nb) * S;
+        for (int j = 0; j < S; j++) {
+            K v = KT<K>::load(b + j);
+            if (KT<K>::eq(v, key)) return 0;
+            if (KT<K>::empty(v)) {
+                b[j] = key;
+                return 1;
+            }
+        }
+    }
+    for (int i = 0; i < kMaxProbe; i++) {
+        const unsigned long long bi = bucket_of(h, i, nb);
+        K *b = table + bi * S;
+        for (int j = 0; j < S; j++) {
+            const K v = KT<K>::load(b + j);
+            const uint64_t hv = KT<K>::hash(v, seed);
+            int iv = -1;
+            for (int q = 0; q < kMaxProbe && iv < 0; q++)
+                if (bucket_of(hv, q, nb) == bi) iv = q;
+            for (int q = iv + 1; iv >= 0 && q < kMaxProbe; q++) {
+                K *bv = table + bucket_of(hv, q, nb) * S;
+                for (int jj = 0; jj < S; jj++) {
+                    if (KT<K>::empty(KT<K>::load(bv + jj))) {
+                        bv[jj] = v;
+                        b[j] = key;
+                        evictions++;
+                        return 1;
+                    }
+                }
+            }
+        }
+    }
+    return 2;
+}
+
+// Place the level's overflowed keys (single thread, table quiescent); new ones
+// are appended to the store.  Sets GPX_ERR_TABLE_FULL when one cannot be placed.
+template <class K>
+__device__ void place_overflow(K *table, unsigned long long nb, K *store, unsigned long long store_cap,
+                               const K *overflow, unsigned long long overflow_cap, Ctrl *c,
+                               unsigned long long seed) {
+    unsigned long long n = c->overflow_count;
+    if (n > overflow_cap) {
+        n = overflow_cap;
+        atomicCAS(&c->error, 0u, (unsigned int)GPX_ERR_TABLE_FULL);
+    }
+    unsigned long long ev = 0;
+    for (unsigned long long k = 0; k < n; k++) {
+        const K key = KT<K>::load(overflow + k);
+        int r = place_evicting<K>(table, nb, key, seed, ev);
+        if (r == 2) {
+            atomicCAS(&c->error, 0u, (unsigned int)GPX_ERR_TABLE_FULL);
+            break;
+        }
+        if (r == 1) {
+            unsigned long long idx = c->store_count++;
+            if (idx < store_cap)
+                store[idx] = key;
+            else
+                atomicCAS(&c->error, 0u, (unsigned int)GPX_ERR_STORE_FULL);
+            c->inserts++;
+        }
+    }
+    c->evictions += ev;
+    c->overflow_count = 0;
+    __threadfence();
 }
 
 // Lookup in a table no one writes to during the call (the decide pass of the
@@ -669,7 +755,13 @@ template <class K, int MODE> struct Explorer {
                 st.lookups++;
                 st.ilookups++;
                 res = find_or_insert<K>(table, P.nbuckets, out, KT<K>::hash(out, P.seed), st.probes);
-                if (res == 2) set_error(P.ctrl, GPX_ERR_TABLE_FULL);
+                if (res == 2) { // full probe sequence: placed with eviction when the level closes
+                    unsigned long long k = atomicAdd(&P.ctrl->overflow_count, 1ull);
+                    if (k < P.overflow_cap)
+                        ((K *)P.overflow)[k] = out;
+                    else
+                        set_error(P.ctrl, GPX_ERR_TABLE_FULL);
+                }
             }
             uint32_t ins = __ballot_sync(kFull, res == 1);
             if (ins) {

@@ -55,13 +55,16 @@ namespace gpx {
 
 // Close the phase that every block has just finished (run by the last block to
 // arrive at the barrier, with all other blocks waiting).
-template <int MODE> __device__ void close_phase(const Params &P) {
+template <class K, int MODE> __device__ void close_phase(const Params &P) {
     Ctrl *c = P.ctrl;
     if (MODE == MODE_PROVISO && c->phase == PH_DECIDE) {
         c->phase = PH_EXPAND;
         c->cursor = 0;
         return;
     }
+    if (c->overflow_count)
+        place_overflow<K>((K *)P.table, P.nbuckets, (K *)P.store, P.store_cap, (const K *)P.overflow, P.overflow_cap,
+                          c, P.seed);
     unsigned long long hi = c->hi;
     unsigned long long newhi = c->store_count;
     if (newhi > P.store_cap) newhi = P.store_cap;
@@ -100,7 +103,7 @@ template <int MODE> __device__ void close_phase(const Params &P) {
 
 // Grid-wide barrier; the last block to arrive closes the phase.  The wait is
 // bounded: after timeout_ns it records GPX_ERR_TIMEOUT and returns.
-template <int MODE> __device__ void grid_barrier(const Params &P) {
+template <class K, int MODE> __device__ void grid_barrier(const Params &P) {
     __syncthreads();
     if (threadIdx.x == 0) {
         Ctrl *c = P.ctrl;
@@ -109,7 +112,7 @@ template <int MODE> __device__ void grid_barrier(const Params &P) {
         unsigned int arrived = atomicAdd(&c->bar_count, 1u);
         if (arrived == gridDim.x - 1) {
             __threadfence();
-            close_phase<MODE>(P);
+            close_phase<K, MODE>(P);
             c->bar_count = 0;
             __threadfence();
             atomicAdd(&c->bar_gen, 1u);
@@ -161,7 +164,7 @@ template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_k
             }
         }
         E.flush_stats();
-        grid_barrier<MODE>(P);
+        grid_barrier<K, MODE>(P);
         if (vload(&c->done) || vload(&c->pause) || vload(&c->error)) break;
     }
 }
@@ -290,6 +293,8 @@ struct gpx_explorer {
     uint32_t *d_model = nullptr;
     size_t model_cap_words = 0;
     uint32_t *d_sel = nullptr;
+    void *d_overflow = nullptr; // keys whose probe sequence was full during a level
+    unsigned long long overflow_cap = 0;
     unsigned long long *d_levels = nullptr;
     unsigned long long *d_scalar = nullptr;
     Ctrl *d_ctrl = nullptr;
@@ -380,6 +385,8 @@ Params make_params(gpx_explorer *ex) {
     P.model_words = (uint32_t)ex->model.dec.words.size();
     P.model_in_smem = ex->model_in_smem;
     P.sel = ex->d_sel;
+    P.overflow = ex->d_overflow;
+    P.overflow_cap = ex->overflow_cap;
     P.levels = ex->d_levels;
     P.ctrl = ex->d_ctrl;
     P.seed = ex->o.seed;
@@ -530,6 +537,7 @@ void gpx_explorer_destroy(gpx_explorer *ex) {
     if (ex->d_store) cudaFree(ex->d_store);
     if (ex->d_model) cudaFree(ex->d_model);
     if (ex->d_sel) cudaFree(ex->d_sel);
+    if (ex->d_overflow) cudaFree(ex->d_overflow);
     if (ex->d_levels) cudaFree(ex->d_levels);
     if (ex->d_scalar) cudaFree(ex->d_scalar);
     if (ex->d_ctrl) cudaFree(ex->d_ctrl);
@@ -588,6 +596,8 @@ int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_exp
     if (cudaMalloc(&ex->d_table, tb) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (cudaMalloc(&ex->d_store, cap * ex->ks.slot_bytes) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (ex->mode == MODE_PROVISO && cudaMalloc(&ex->d_sel, cap * 4) != cudaSuccess) return fail(GPX_ERR_NOMEM);
+    ex->overflow_cap = 1u << 16;
+    if (cudaMalloc(&ex->d_overflow, ex->overflow_cap * ex->ks.slot_bytes) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (cudaMalloc(&ex->d_levels, (size_t)kMaxLevels * 8) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (cudaMalloc(&ex->d_scalar, 64) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (cudaMalloc(&ex->d_ctrl, sizeof(Ctrl)) != cudaSuccess) return fail(GPX_ERR_NOMEM);
@@ -698,6 +708,7 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     r->transitions = c.inserts_lookups; // successors sent to the table for insertion
     r->probes = c.probes;
     r->inserts = c.inserts;
+    r->evictions = c.evictions;
     r->expanded = c.expanded;
     r->launches = launches;
     r->kernel_ms = kernel_ms;
@@ -989,6 +1000,7 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     // carve the array
     const size_t total = GPX_NOALLOC_SCRATCH_BYTES;
     const size_t off_ctrl = 0, off_scalar = 256, off_levels = 4096;
+    static_assert(sizeof(Ctrl) <= 256, "the control block must fit below the scalar slot");
     const size_t off_model = round_up(off_levels + (size_t)kMaxLevels * 8, 256);
     const size_t model_bytes = model->dec.words.size() * 4;
     const size_t off_table = round_up(off_model + model_bytes, 256);

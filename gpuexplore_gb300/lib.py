@@ -83,7 +83,7 @@ class Result(C.Structure):
         ("key_words", C.c_uint32), ("table_count", C.c_uint64), ("lookups", C.c_uint64),
         ("expanded", C.c_uint64), ("kernel_ms", C.c_double), ("states_buf", C.POINTER(C.c_uint32)),
         ("table_slots", C.c_uint64), ("slot_bytes", C.c_uint32), ("blocks", C.c_uint32), ("threads", C.c_uint32),
-        ("inserts", C.c_uint64),
+        ("inserts", C.c_uint64), ("evictions", C.c_uint64),
     ]
 
 
@@ -261,7 +261,7 @@ def _result_dict(r: Result) -> Dict:
         "status": int(r.status), "stopped": STOPS[r.stopped] if 0 <= r.stopped < 4 else str(r.stopped),
         "verdict": VERDICTS.get(int(r.verdict), str(r.verdict)), "states": int(r.states), "levels": levels,
         "transitions": int(r.transitions), "probes": int(r.probes), "lookups": int(r.lookups),
-        "inserts": int(r.inserts),
+        "inserts": int(r.inserts), "evictions": int(r.evictions),
         "expanded": int(r.expanded), "launches": int(r.launches), "explore_ms": float(r.explore_ms),
         "kernel_ms": float(r.kernel_ms), "setup_ms": float(r.setup_ms), "set_hash": f"{r.set_hash:016x}",
         "key_words": int(r.key_words), "table_count": int(r.table_count), "table_slots": int(r.table_slots),

@@ -100,6 +100,7 @@ typedef struct {
     uint32_t slot_bytes;     /* bytes per hash-table slot (4, 8 or 16) */
     uint32_t blocks, threads;/* launch configuration that ran */
     uint64_t inserts;        /* states inserted into the hash table by the exploration kernels */
+    uint64_t evictions;      /* stored states displaced within their probe sequence to make room */
 } gpx_result;
 
 typedef struct gpx_model gpx_model;

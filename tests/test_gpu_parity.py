@@ -86,3 +86,22 @@ def test_full_set_rows(gpu, tmp_path):
     assert g["table_count"] == g["states"]
     # BFS order: level boundaries of the store match the per-level counts
     assert got.shape[0] == sum(g["levels"])
+
+
+@pytest.mark.parametrize("slots_per_state", [1.06, 1.15])
+def test_high_load_bounded_eviction(gpu, tmp_path, slots_per_state):
+    """A table barely larger than the state space: inserts whose probe sequence is
+    full displace an occupant to a later slot of its own sequence; the visited set
+    stays exact."""
+    net = gen.random_network(41, nprocs=28, states=(3, 6), outdeg=(1, 2), safety=False)
+    assert net.firstbit()[-1] > 63  # 128-bit slots: 2 per bucket, the tightest case
+    path = write_net(net, tmp_path, "dense")
+    o = oracle(path, [], max_states=200_000)
+    slots = int(o["states"] * slots_per_state)
+    q_words = (slots * 16) // 4
+    g = _gpu(gpu, path, {}, max_states=200_000, q_words=q_words, store_states=o["states"] + 64,
+             collect_states=1)
+    _same(o, g)
+    assert g["table_count"] == g["states"]  # every state stored exactly once
+    if slots_per_state < 1.1:
+        assert g["evictions"] > 0
