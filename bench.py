@@ -383,8 +383,8 @@ def main():
                    "blocks": r["blocks"],
                    "threads": r["threads"], "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (20 GB table, re-initialised every step)"},
-        "e2e": {"value": e2e, "unit": "states/s", "h2d_bytes_per_step": h2d + 160,
-                "d2h_bytes_per_step": 8 * len(r["levels"]) + 16 + 160},
+        "e2e": {"value": e2e, "unit": "states/s", "h2d_bytes_per_step": h2d + r2["h2d_bytes"],
+                "d2h_bytes_per_step": r2["d2h_bytes"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                      "peak_source": f"{peak_kind} hbm_gbs", "kernel": "explore_kernel",
@@ -397,7 +397,8 @@ def main():
                                        "how": "gpx_random_gather_probe: random 32 B sectors over 20 GB, "
                                               "the probe's load instruction"}},
         "clocks": clk,
-        "gpu_launches": sum(x["launches"] + 2 for x in results),
+        # per run: init, the exploration launches, one relaunch test after each, set hash
+        "gpu_launches": sum(2 * x["launches"] + 2 for x in results),
         "hash_probe_gbs": 32 * r["probes"] / (kms / 1000.0) / 1e9,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

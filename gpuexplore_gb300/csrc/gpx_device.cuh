@@ -20,16 +20,19 @@ constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr int kPairMax = 256;   // (state, process) pairs staged per warp batch
 constexpr int kMaxProbe = 32;   // buckets probed before reporting the table full
 constexpr uint32_t kMaxLevels = 1u << 20;
+constexpr unsigned long long kMaxLaunches = 2ull * kMaxLevels; // exploration launches per run
 
 enum Mode : int { MODE_PLAIN = 0, MODE_POR = 1, MODE_PROVISO = 2 };
 enum Phase : uint32_t { PH_EXPAND = 0, PH_DECIDE = 1 };
 
 // Control block shared by all blocks of the persistent kernel.
-struct Ctrl {
-    unsigned long long store_count; // states appended to the store
+// Run control block.  Fields that many warps touch during a level sit on
+// separate 128-byte lines: the level parameters (written only by the thread
+// that closes a phase), the claim cursor, the store append counter, the two
+// barrier words and the statistics, so polling and atomics on one do not queue
+// behind the others in the same L2 slice.
+struct alignas(128) Ctrl {
     unsigned long long lo, hi;      // the level being expanded: store indices [lo, hi)
-    unsigned long long cursor;      // next unclaimed offset within [lo, hi)
-    unsigned long long lookups, probes, expanded, inserts, inserts_lookups;
     unsigned int claim;             // states per claim
     unsigned int level;             // BFS depth of [lo, hi)
     unsigned int nlevels;           // recorded level counts
@@ -40,10 +43,16 @@ struct Ctrl {
     unsigned int stop;              // gpx_stop
     unsigned int phase;             // Phase
     unsigned int launch_levels;     // levels closed in this launch
-    unsigned int bar_count, bar_gen;
     unsigned int timeout_at;        // where a bounded wait gave up (diagnostics)
     unsigned long long overflow_count; // keys whose probe sequence was full during this level
     unsigned long long evictions;      // keys displaced to make room
+    unsigned long long launches;       // exploration launches of a graph-driven run
+    alignas(128) unsigned long long cursor;      // dynamic claims: offset beyond the static first claims
+    alignas(128) unsigned long long store_count; // states appended to the store
+    alignas(128) unsigned int bar_count;         // grid barrier arrivals
+    alignas(128) unsigned int bar_gen;           // grid barrier generation (polled by waiting blocks)
+    alignas(128) unsigned long long lookups; // statistics (one line)
+    unsigned long long probes, expanded, inserts, inserts_lookups;
 };
 
 struct Params {
@@ -451,12 +460,13 @@ static __device__ __forceinline__ unsigned long long vload(const unsigned long l
 
 // Spin (with back-off) until *word differs from `old`, for at most timeout_ns.
 // Returns false when the limit ran out: every device-side wait here ends.
-static __device__ __forceinline__ bool wait_change(const unsigned int *word, unsigned int old, unsigned long long timeout_ns) {
+static __device__ __forceinline__ bool wait_change(const unsigned int *word, unsigned int old, unsigned long long timeout_ns,
+                                                   unsigned int max_sleep_ns = 1024) {
     uint64_t t0 = globaltimer();
     unsigned int ns = 32;
     while (vload(word) == old) {
         __nanosleep(ns);
-        if (ns < 1024) ns <<= 1;
+        if (ns < max_sleep_ns) ns <<= 1;
         if (globaltimer() - t0 > timeout_ns) return false;
     }
     return true;
@@ -921,23 +931,35 @@ template <class K, int MODE> struct Explorer {
         __syncwarp();
     }
 
-    __device__ void flush_stats() {
+    // End of a level: append the staged new states and report a violation.
+    // The counters stay in registers (flushed by flush_counters) unless a lane
+    // nears the range of its 32-bit counts.
+    __device__ void flush_level() {
         if (scount) stage_flush(scount);
+        if (__any_sync(kFull, st.violation) && lane == 0) atomicOr(&P.ctrl->violation, 1u);
+        st.violation = 0;
+        if (__any_sync(kFull, st.probes > (1u << 30) || st.lookups > (1u << 30))) flush_counters();
+    }
+
+    __device__ void flush_counters() {
         Ctrl *c = P.ctrl;
-        unsigned int v[5] = {st.lookups, st.probes, st.inserts, st.expanded, st.ilookups};
+        unsigned long long v[5] = {st.lookups, st.probes, st.inserts, st.expanded, st.ilookups};
 #pragma unroll
         for (int k = 0; k < 5; k++)
             for (int o = 16; o; o >>= 1) v[k] += __shfl_xor_sync(kFull, v[k], o);
-        unsigned int viol = __any_sync(kFull, st.violation);
         if (lane == 0) {
-            if (v[0]) atomicAdd(&c->lookups, (unsigned long long)v[0]);
-            if (v[1]) atomicAdd(&c->probes, (unsigned long long)v[1]);
-            if (v[2]) atomicAdd(&c->inserts, (unsigned long long)v[2]);
-            if (v[3]) atomicAdd(&c->expanded, (unsigned long long)v[3]);
-            if (v[4]) atomicAdd(&c->inserts_lookups, (unsigned long long)v[4]);
-            if (viol) atomicOr(&c->violation, 1u);
+            if (v[0]) atomicAdd(&c->lookups, v[0]);
+            if (v[1]) atomicAdd(&c->probes, v[1]);
+            if (v[2]) atomicAdd(&c->inserts, v[2]);
+            if (v[3]) atomicAdd(&c->expanded, v[3]);
+            if (v[4]) atomicAdd(&c->inserts_lookups, v[4]);
         }
-        st = WarpStats{0, 0, 0, 0, 0, 0};
+        st = WarpStats{0, 0, 0, 0, 0, st.violation};
+    }
+
+    __device__ void flush_stats() {
+        flush_level();
+        flush_counters();
     }
 };
 

@@ -101,9 +101,25 @@ template <class K, int MODE> __device__ void close_phase(const Params &P) {
     if (P.levels_per_launch && c->launch_levels >= P.levels_per_launch && !c->done) c->pause = 1;
 }
 
+// What a block needs of the current phase, read from the control block once
+// per block (by the barrier thread) instead of by every warp.
+struct LevelView {
+    unsigned long long lo, hi;
+    unsigned int claim, phase, stop;
+};
+
+__device__ __forceinline__ void read_view(const Ctrl *c, LevelView &v) {
+    v.lo = vload(&c->lo);
+    v.hi = vload(&c->hi);
+    v.claim = vload(&c->claim);
+    v.phase = vload(&c->phase);
+    v.stop = vload(&c->done) | vload(&c->pause) | vload(&c->error);
+}
+
 // Grid-wide barrier; the last block to arrive closes the phase.  The wait is
-// bounded: after timeout_ns it records GPX_ERR_TIMEOUT and returns.
-template <class K, int MODE> __device__ void grid_barrier(const Params &P) {
+// bounded: after timeout_ns it records GPX_ERR_TIMEOUT and returns.  Thread 0
+// then refreshes the block's view of the next phase.
+template <class K, int MODE> __device__ void grid_barrier(const Params &P, LevelView &view) {
     __syncthreads();
     if (threadIdx.x == 0) {
         Ctrl *c = P.ctrl;
@@ -116,17 +132,19 @@ template <class K, int MODE> __device__ void grid_barrier(const Params &P) {
             c->bar_count = 0;
             __threadfence();
             atomicAdd(&c->bar_gen, 1u);
-        } else if (!wait_change(&c->bar_gen, gen, P.timeout_ns)) {
+        } else if (!wait_change(&c->bar_gen, gen, P.timeout_ns, 512)) {
             set_error(c, GPX_ERR_TIMEOUT);
             atomicMax(&c->timeout_at, 1u);
         }
         __threadfence();
+        read_view(c, view);
     }
     __syncthreads();
 }
 
 template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_kernel(Params P) {
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ LevelView view;
     const uint32_t *model = P.model;
     size_t model_bytes = 0;
     if (P.model_in_smem) {
@@ -137,41 +155,56 @@ template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_k
     }
     WarpScratch<K, MODE> *wsall = (WarpScratch<K, MODE> *)(smem + model_bytes);
     WarpScratch<K, MODE> &ws = wsall[threadIdx.x >> 5];
+    Ctrl *c = P.ctrl;
+    if (threadIdx.x == 0) read_view(c, view);
     __syncthreads();
 
     Explorer<K, MODE> E(P, model, ws);
-    Ctrl *c = P.ctrl;
     const uint32_t n = E.M.n;
     uint32_t Bmax = kPairMax / n;
     if (Bmax > 32) Bmax = 32;
     if (Bmax < 1) Bmax = 1;
-    for (;;) {
-        unsigned long long lo = vload(&c->lo), hi = vload(&c->hi);
-        unsigned int claim = vload(&c->claim);
+    // every warp's first claim of a phase is static (warp gw takes
+    // [gw * claim, (gw + 1) * claim)); the cursor hands out the rest
+    const unsigned long long gw = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    while (!view.stop) {
+        const unsigned long long lo = view.lo, nlev = view.hi - view.lo;
+        const unsigned int claim = view.claim;
         const uint32_t B = claim < Bmax ? claim : Bmax;
-        bool decide = (MODE == MODE_PROVISO) && vload(&c->phase) == PH_DECIDE;
-        unsigned long long nlev = hi - lo;
-        for (;;) {
-            unsigned long long base = nlev;
-            // read before contending: on small levels most warps find nothing to claim
-            if (E.lane == 0 && vload(&c->cursor) < nlev) base = atomicAdd(&c->cursor, (unsigned long long)claim);
-            base = __shfl_sync(kFull, base, 0);
-            if (base >= nlev || vload(&c->error)) break;
+        const bool decide = (MODE == MODE_PROVISO) && view.phase == PH_DECIDE;
+        const unsigned long long static_end = (unsigned long long)P.total_warps * claim;
+        unsigned long long base = gw * claim;
+        while (base < nlev) {
             unsigned long long end = base + claim < nlev ? base + claim : nlev;
             for (unsigned long long b = base; b < end; b += B) {
                 uint32_t cnt = (uint32_t)((end - b) < B ? (end - b) : B);
                 E.batch(lo + b, cnt, b, decide);
             }
+            if (static_end >= nlev) break;
+            base = nlev;
+            // read before contending: late in a level most warps find nothing to claim
+            if (E.lane == 0 && static_end + vload(&c->cursor) < nlev && !vload(&c->error))
+                base = static_end + atomicAdd(&c->cursor, (unsigned long long)claim);
+            base = __shfl_sync(kFull, base, 0);
         }
-        E.flush_stats();
-        grid_barrier<K, MODE>(P);
-        if (vload(&c->done) || vload(&c->pause) || vload(&c->error)) break;
+        E.flush_level();
+        grid_barrier<K, MODE>(P, view);
     }
+    E.flush_counters();
 }
 
-// Insert the all-zero initial state (GPUexplore.cu:668-682).
-template <class K> __global__ void init_kernel(Params P) {
+// Reset the control block to level 0 = {initial state} and insert the
+// all-zero initial state (GPUexplore.cu:668-682).
+template <class K> __global__ void init_kernel(Params P, unsigned int first_phase) {
+    Ctrl *c = P.ctrl;
+    for (unsigned int i = threadIdx.x; i < sizeof(Ctrl) / 4; i += blockDim.x) ((unsigned int *)c)[i] = 0;
+    __syncthreads();
     if (threadIdx.x != 0) return;
+    c->store_count = 1;
+    c->hi = 1;
+    c->nlevels = 1;
+    c->claim = 1;
+    c->phase = first_phase;
     K key = KT<K>::initial();
     unsigned int probes = 0;
     find_or_insert<K>((K *)P.table, P.nbuckets, key, KT<K>::hash(key, P.seed), probes);
@@ -179,11 +212,34 @@ template <class K> __global__ void init_kernel(Params P) {
     P.levels[0] = 1;
 }
 
+// After the last exploration launch of a graph-driven run: decide on the
+// device whether another launch follows (the host relaunch loop's test,
+// without the round trip), and rearm the -k budget if so.
+__global__ void relaunch_kernel(Ctrl *c, cudaGraphConditionalHandle loop) {
+    unsigned int more = !(c->done || c->error);
+    c->launches++;
+    if (more && c->launches >= kMaxLaunches) { // unreachable: each launch closes >= 1 of <= kMaxLevels levels
+        set_error(c, GPX_ERR_UNSUPPORTED);
+        c->done = 1;
+        c->stop = GPX_STOP_ERROR;
+        more = 0;
+    }
+    if (more) {
+        c->pause = 0;
+        c->launch_levels = 0;
+    }
+    __threadfence();
+    cudaGraphSetConditional(loop, more);
+}
+
 // Order-independent hash of the visited set over the state-vector words
-// (the sum of per-state key hashes; the oracle computes the same sum).
+// (the sum of per-state key hashes; the oracle computes the same sum).  The
+// state count is `count`, or min(*count_dev, cap) when count_dev is given (a
+// graph captured before the count is known).
 template <class K>
-__global__ void set_hash_kernel(const K *store, unsigned long long count, uint32_t words,
-                                unsigned long long *out) {
+__global__ void set_hash_kernel(const K *store, unsigned long long count, const unsigned long long *count_dev,
+                                unsigned long long cap, uint32_t words, unsigned long long *out) {
+    if (count_dev) count = *count_dev < cap ? *count_dev : cap;
     unsigned long long acc = 0;
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < count;
          i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -245,13 +301,31 @@ const char *kStatusStrings[] = {"ok",
 
 struct KernelSet {
     void (*explore[3])(Params);
-    void (*init)(Params);
+    void (*init)(Params, unsigned int);
+    void (*set_hash)(cudaStream_t, int blocks, const void *store, unsigned long long count,
+                     const unsigned long long *count_dev, unsigned long long cap, uint32_t words,
+                     unsigned long long *out);
+    void (*count)(cudaStream_t, int blocks, const void *table, unsigned long long slots, unsigned long long *out);
     size_t scratch_bytes[3];
     uint32_t slot_bytes, bucket_slots;
 };
 
+template <class K>
+void launch_set_hash(cudaStream_t st, int blocks, const void *store, unsigned long long count,
+                     const unsigned long long *count_dev, unsigned long long cap, uint32_t words,
+                     unsigned long long *out) {
+    set_hash_kernel<K><<<blocks, 256, 0, st>>>((const K *)store, count, count_dev, cap, words, out);
+}
+
+template <class K>
+void launch_count(cudaStream_t st, int blocks, const void *table, unsigned long long slots, unsigned long long *out) {
+    count_kernel<K><<<blocks, 256, 0, st>>>((const K *)table, slots, out);
+}
+
 template <class K> KernelSet kernels_for() {
     KernelSet s;
+    s.set_hash = launch_set_hash<K>;
+    s.count = launch_count<K>;
     s.explore[0] = explore_kernel<K, MODE_PLAIN>;
     s.explore[1] = explore_kernel<K, MODE_POR>;
     s.explore[2] = explore_kernel<K, MODE_PROVISO>;
@@ -274,6 +348,19 @@ template <class K> KernelSet kernels_for() {
     } while (0)
 
 } // namespace
+
+// Everything a captured run depends on: the graph is replayed while it is unchanged.
+struct GraphKey {
+    Params P;
+    void (*kern)(Params);
+    int blocks, threads;
+    size_t smem;
+    unsigned int first_phase;
+    uint32_t key_words;
+    int collect;
+    void *log_count;
+};
+constexpr uint32_t kGraphLevels = 4096; // level counts read back by the graph itself
 
 struct gpx_explorer {
     gpx_options o;
@@ -310,6 +397,13 @@ struct gpx_explorer {
     unsigned long long *d_log_count = nullptr;
     unsigned long long log_cap = 0;
     uint32_t log_every = 0;
+    // a run as one CUDA graph (launch_graph), rebuilt when its key changes
+    GraphKey graph_key;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaStream_t st_body = nullptr;          // captures the body of the launch loop
+    unsigned long long *h_levels = nullptr;  // pinned: the first kGraphLevels level counts
+    unsigned long long *h_scalar = nullptr;  // pinned: set hash, table count
 };
 
 namespace {
@@ -406,6 +500,135 @@ Params make_params(gpx_explorer *ex) {
     return P;
 }
 
+int count_blocks(const gpx_explorer *ex) {
+    return (int)std::max<unsigned long long>(1, std::min<unsigned long long>((ex->slots + 255) / 256, 8192));
+}
+
+void destroy_graph(gpx_explorer *ex) {
+    if (ex->graph_exec) cudaGraphExecDestroy(ex->graph_exec);
+    if (ex->graph) cudaGraphDestroy(ex->graph);
+    ex->graph_exec = nullptr;
+    ex->graph = nullptr;
+}
+
+GraphKey graph_key(const gpx_explorer *ex, const Params &P, unsigned int first_phase) {
+    GraphKey k;
+    memset(&k, 0, sizeof k);
+    k.P = P;
+    k.kern = ex->ks.explore[ex->mode];
+    k.blocks = ex->blocks;
+    k.threads = ex->threads;
+    k.smem = ex->smem;
+    k.first_phase = first_phase;
+    k.key_words = ex->model.dec.key_words;
+    k.collect = (ex->o.collect_states || ex->o.verbosity >= 2) ? 1 : 0;
+    k.log_count = ex->d_log_count;
+    return k;
+}
+
+// Record one run into a graph on ex->st:
+//   reset table + init -> while (more) { exploration launch; relaunch_kernel } -> set hash -> read-back
+// The loop's condition is set on the device by relaunch_kernel, so a -k run
+// needs no host round trip between launches.
+cudaError_t capture_run(gpx_explorer *ex, const GraphKey &k, cudaGraph_t *out) {
+    cudaStream_t st = ex->st, sb = ex->st_body;
+    bool body_open = false;
+    auto record = [&]() -> cudaError_t {
+        cudaError_t e;
+#define GPX_CAP(call)                                                                                         \
+    do {                                                                                                      \
+        if ((e = (call)) != cudaSuccess) return e;                                                            \
+    } while (0)
+        Params P = k.P;
+        GPX_CAP(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        GPX_CAP(cudaEventRecordWithFlags(ex->ev[0], st, cudaEventRecordExternal));
+        GPX_CAP(cudaMemsetAsync(ex->d_table, 0, ex->table_bytes, st));
+        if (k.log_count) GPX_CAP(cudaMemsetAsync(k.log_count, 0, 8, st));
+        ex->ks.init<<<1, 32, 0, st>>>(P, k.first_phase);
+        GPX_CAP(cudaGetLastError());
+        GPX_CAP(cudaEventRecordWithFlags(ex->ev[1], st, cudaEventRecordExternal));
+
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t *deps = nullptr;
+        const cudaGraphEdgeData *edges = nullptr;
+        size_t ndeps = 0;
+        GPX_CAP(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &edges, &ndeps));
+        cudaGraphConditionalHandle loop;
+        GPX_CAP(cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams np = {cudaGraphNodeTypeConditional}; // the rest zero-initialised
+        np.conditional.handle = loop;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        GPX_CAP(cudaGraphAddNode(&node, g, deps, edges, ndeps, &np));
+        GPX_CAP(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        GPX_CAP(cudaStreamBeginCaptureToGraph(sb, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal));
+        body_open = true;
+        void *args[] = {&P};
+        GPX_CAP(cudaLaunchCooperativeKernel((const void *)k.kern, dim3(k.blocks), dim3(k.threads), args, k.smem, sb));
+        relaunch_kernel<<<1, 1, 0, sb>>>(ex->d_ctrl, loop);
+        GPX_CAP(cudaGetLastError());
+        cudaGraph_t body = nullptr; // owned by the conditional node
+        body_open = false;
+        GPX_CAP(cudaStreamEndCapture(sb, &body));
+
+        GPX_CAP(cudaEventRecordWithFlags(ex->ev[3], st, cudaEventRecordExternal));
+        GPX_CAP(cudaMemsetAsync(ex->d_scalar, 0, 16, st));
+        int hb = (int)std::max<unsigned long long>(1, std::min<unsigned long long>((ex->store_cap + 255) / 256, 4096));
+        ex->ks.set_hash(st, hb, ex->d_store, 0, &ex->d_ctrl->store_count, ex->store_cap, k.key_words, ex->d_scalar);
+        if (k.collect) ex->ks.count(st, count_blocks(ex), ex->d_table, ex->slots, ex->d_scalar + 1);
+        GPX_CAP(cudaGetLastError());
+        GPX_CAP(cudaMemcpyAsync(ex->h_ctrl, ex->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));
+        GPX_CAP(cudaMemcpyAsync(ex->h_scalar, ex->d_scalar, 16, cudaMemcpyDeviceToHost, st));
+        GPX_CAP(cudaMemcpyAsync(ex->h_levels, ex->d_levels, (size_t)kGraphLevels * 8, cudaMemcpyDeviceToHost, st));
+#undef GPX_CAP
+        return cudaStreamEndCapture(st, out);
+    };
+    cudaError_t e = record();
+    if (e != cudaSuccess) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaGraph_t t = nullptr;
+        if (body_open) cudaStreamEndCapture(sb, &t);
+        if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+            t = nullptr;
+            cudaStreamEndCapture(st, &t);
+            if (t) cudaGraphDestroy(t);
+        }
+        cudaGetLastError();
+    }
+    return e;
+}
+
+// Run the exploration as one graph launch (built on first use or when the key changed).
+int run_graph(gpx_explorer *ex, const Params &P, unsigned int first_phase) {
+    GraphKey k = graph_key(ex, P, first_phase);
+    if (!ex->graph_exec || memcmp(&k, &ex->graph_key, sizeof k) != 0) {
+        destroy_graph(ex);
+        if (!ex->st_body) GPX_CUDA(cudaStreamCreateWithFlags(&ex->st_body, cudaStreamNonBlocking));
+        if (!ex->h_levels) GPX_CUDA(cudaMallocHost(&ex->h_levels, (size_t)kGraphLevels * 8));
+        if (!ex->h_scalar) GPX_CUDA(cudaMallocHost(&ex->h_scalar, 16));
+        cudaGraph_t g = nullptr;
+        cudaError_t e = capture_run(ex, k, &g);
+        if (e == cudaSuccess) {
+            ex->graph = g;
+            e = cudaGraphInstantiate(&ex->graph_exec, g, 0);
+        }
+        if (e != cudaSuccess) {
+            fprintf(stderr, "gpx: building the run graph failed: %s (launch_graph = 0 runs without it)\n",
+                    cudaGetErrorString(e));
+            destroy_graph(ex);
+            cudaGetLastError();
+            return GPX_ERR_CUDA;
+        }
+        ex->graph_key = k;
+    }
+    GPX_CUDA(cudaGraphLaunch(ex->graph_exec, ex->st));
+    GPX_CUDA(cudaStreamSynchronize(ex->st));
+    return GPX_OK;
+}
+
 void print_states(FILE *out, gpx_explorer *ex, const std::vector<uint32_t> &words, unsigned long long count,
                   unsigned long long unexplored_from) {
     const Gpf &g = ex->model.gpf;
@@ -484,6 +707,7 @@ void gpx_options_init(gpx_options *o) {
     memset(o, 0, sizeof *o);
     o->struct_size = sizeof *o;
     o->seed = 0x243F6A8885A308D3ull;
+    o->launch_graph = 1;
 }
 
 int gpx_model_load(const char *path_without_ext, gpx_model **out) {
@@ -533,6 +757,10 @@ void gpx_model_free(gpx_model *m) { delete m; }
 
 void gpx_explorer_destroy(gpx_explorer *ex) {
     if (!ex) return;
+    destroy_graph(ex);
+    if (ex->st_body) cudaStreamDestroy(ex->st_body);
+    if (ex->h_levels) cudaFreeHost(ex->h_levels);
+    if (ex->h_scalar) cudaFreeHost(ex->h_scalar);
     if (ex->d_table) cudaFree(ex->d_table);
     if (ex->d_store) cudaFree(ex->d_store);
     if (ex->d_model) cudaFree(ex->d_model);
@@ -553,6 +781,7 @@ void gpx_explorer_destroy(gpx_explorer *ex) {
 
 int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_explorer **out) {
     if (!model || !opts || !out || opts->struct_size != sizeof(gpx_options)) return GPX_ERR_INVALID;
+    if (opts->bucket_bytes != 0 && opts->bucket_bytes != 32) return GPX_ERR_INVALID;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPX_ERR_NO_GPU;
     if (opts->device < 0 || opts->device >= ndev) return GPX_ERR_INVALID;
@@ -624,27 +853,7 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     r->struct_size = sizeof *r;
     if (cudaSetDevice(ex->o.device) != cudaSuccess) return GPX_ERR_CUDA;
     Params P = make_params(ex);
-    // reset: empty table, empty store, initial state (GPUexplore.cu:2091-2092)
-    GPX_CUDA(cudaEventRecord(ex->ev[0], ex->st));
-    GPX_CUDA(cudaMemsetAsync(ex->d_table, 0, ex->table_bytes, ex->st));
-    Ctrl c0;
-    memset(&c0, 0, sizeof c0);
-    c0.store_count = 1;
-    c0.lo = 0;
-    c0.hi = 1;
-    c0.nlevels = 1;
-    c0.claim = 1;
-    c0.phase = ex->mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND;
-    *ex->h_ctrl = c0;
-    GPX_CUDA(cudaMemcpyAsync(ex->d_ctrl, ex->h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, ex->st));
-    if (ex->d_log_count) GPX_CUDA(cudaMemsetAsync(ex->d_log_count, 0, 8, ex->st));
-    ex->ks.init<<<1, 32, 0, ex->st>>>(P);
-    GPX_CUDA(cudaGetLastError());
-    GPX_CUDA(cudaEventRecord(ex->ev[1], ex->st));
-    void (*kern)(Params) = ex->ks.explore[ex->mode];
-    void *args[] = {&P};
-    unsigned long long launches = 0;
-    float kernel_ms = 0;
+    const unsigned int first_phase = ex->mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND;
     // Hash probes are random 32-byte reads: ask L2 to fetch no more than a sector
     // per miss (unset, a miss fills 128 bytes; the request rate is the same either
     // way, the DRAM traffic is not).  The caller's limit is restored afterwards.
@@ -658,42 +867,64 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
             if (on) cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, v);
         }
     } fetch_restore{restore_fetch, saved_fetch};
-    for (;;) {
-        GPX_CUDA(cudaEventRecord(ex->ev[2], ex->st));
-        GPX_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(ex->blocks), dim3(ex->threads), args, ex->smem,
-                                             ex->st));
-        GPX_CUDA(cudaEventRecord(ex->ev[3], ex->st));
-        launches++;
-        GPX_CUDA(cudaMemcpyAsync(ex->h_ctrl, ex->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, ex->st));
-        GPX_CUDA(cudaStreamSynchronize(ex->st));
-        float ms = 0;
-        cudaEventElapsedTime(&ms, ex->ev[2], ex->ev[3]);
-        kernel_ms += ms;
-        Ctrl &c = *ex->h_ctrl;
-        if (ex->o.verbosity == 1) printf("%llu\n", launches - 1);
-        if (ex->o.verbosity >= 2) {
-            unsigned long long cnt = std::min<unsigned long long>(c.store_count, ex->store_cap);
-            if (ex->o.verbosity == 2) {
-                printf("nr. of states in hash table: %llu (%llu unexplored states)\n", cnt, cnt - c.lo);
-            } else {
-                std::vector<uint32_t> w;
-                int rc = collect_words(ex, cnt, &w);
-                if (rc != GPX_OK) return rc;
-                print_states(stdout, ex, w, cnt, c.lo);
+    unsigned long long launches = 0;
+    float kernel_ms = 0, setup_ms = 0, total_ms = 0;
+    // -v prints between launches, so it keeps the host loop
+    const bool graph = ex->o.launch_graph && ex->o.verbosity <= 0;
+    if (graph) {
+        int rc = run_graph(ex, P, first_phase);
+        if (rc != GPX_OK) return rc;
+        launches = ex->h_ctrl->launches;
+        cudaEventElapsedTime(&setup_ms, ex->ev[0], ex->ev[1]);
+        cudaEventElapsedTime(&kernel_ms, ex->ev[1], ex->ev[3]);
+        total_ms = kernel_ms;
+    } else {
+        // reset: empty table, empty store, initial state (GPUexplore.cu:2091-2092)
+        GPX_CUDA(cudaEventRecord(ex->ev[0], ex->st));
+        GPX_CUDA(cudaMemsetAsync(ex->d_table, 0, ex->table_bytes, ex->st));
+        if (ex->d_log_count) GPX_CUDA(cudaMemsetAsync(ex->d_log_count, 0, 8, ex->st));
+        ex->ks.init<<<1, 32, 0, ex->st>>>(P, first_phase);
+        GPX_CUDA(cudaGetLastError());
+        GPX_CUDA(cudaEventRecord(ex->ev[1], ex->st));
+        void (*kern)(Params) = ex->ks.explore[ex->mode];
+        void *args[] = {&P};
+        for (;;) {
+            GPX_CUDA(cudaEventRecord(ex->ev[2], ex->st));
+            GPX_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(ex->blocks), dim3(ex->threads), args,
+                                                 ex->smem, ex->st));
+            GPX_CUDA(cudaEventRecord(ex->ev[3], ex->st));
+            launches++;
+            GPX_CUDA(cudaMemcpyAsync(ex->h_ctrl, ex->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, ex->st));
+            GPX_CUDA(cudaStreamSynchronize(ex->st));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ex->ev[2], ex->ev[3]);
+            kernel_ms += ms;
+            Ctrl &c = *ex->h_ctrl;
+            if (ex->o.verbosity == 1) printf("%llu\n", launches - 1);
+            if (ex->o.verbosity >= 2) {
+                unsigned long long cnt = std::min<unsigned long long>(c.store_count, ex->store_cap);
+                if (ex->o.verbosity == 2) {
+                    printf("nr. of states in hash table: %llu (%llu unexplored states)\n", cnt, cnt - c.lo);
+                } else {
+                    std::vector<uint32_t> w;
+                    int rc = collect_words(ex, cnt, &w);
+                    if (rc != GPX_OK) return rc;
+                    print_states(stdout, ex, w, cnt, c.lo);
+                }
             }
+            if (c.done || c.error) break;
+            // -k budget reached: resume with a fresh launch
+            c.pause = 0;
+            c.launch_levels = 0;
+            GPX_CUDA(cudaMemcpyAsync(&ex->d_ctrl->pause, &c.pause, sizeof(unsigned int), cudaMemcpyHostToDevice,
+                                     ex->st));
+            GPX_CUDA(cudaMemcpyAsync(&ex->d_ctrl->launch_levels, &c.launch_levels, sizeof(unsigned int),
+                                     cudaMemcpyHostToDevice, ex->st));
         }
-        if (c.done || c.error) break;
-        // -k budget reached: resume with a fresh launch
-        c.pause = 0;
-        c.launch_levels = 0;
-        GPX_CUDA(cudaMemcpyAsync(&ex->d_ctrl->pause, &c.pause, sizeof(unsigned int), cudaMemcpyHostToDevice, ex->st));
-        GPX_CUDA(cudaMemcpyAsync(&ex->d_ctrl->launch_levels, &c.launch_levels, sizeof(unsigned int),
-                                 cudaMemcpyHostToDevice, ex->st));
+        cudaEventElapsedTime(&setup_ms, ex->ev[0], ex->ev[1]);
+        cudaEventElapsedTime(&total_ms, ex->ev[1], ex->ev[3]);
     }
     Ctrl &c = *ex->h_ctrl;
-    float setup_ms = 0, total_ms = 0;
-    cudaEventElapsedTime(&setup_ms, ex->ev[0], ex->ev[1]);
-    cudaEventElapsedTime(&total_ms, ex->ev[1], ex->ev[3]);
     r->status = c.error ? (int)c.error : GPX_OK;
     r->stopped = (int)c.stop;
     if (c.error) r->stopped = GPX_STOP_ERROR;
@@ -702,8 +933,6 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     r->states = count;
     r->nlevels = c.nlevels;
     r->level_counts = (uint64_t *)malloc(sizeof(uint64_t) * std::max(1u, c.nlevels));
-    GPX_CUDA(cudaMemcpyAsync(r->level_counts, ex->d_levels, sizeof(uint64_t) * c.nlevels, cudaMemcpyDeviceToHost,
-                             ex->st));
     r->lookups = c.lookups;
     r->transitions = c.inserts_lookups; // successors sent to the table for insertion
     r->probes = c.probes;
@@ -719,35 +948,34 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     r->slot_bytes = ex->ks.slot_bytes;
     r->blocks = (uint32_t)ex->blocks;
     r->threads = (uint32_t)ex->threads;
-    // set hash over the visited states
-    GPX_CUDA(cudaMemsetAsync(ex->d_scalar, 0, 16, ex->st));
-    {
+    if (graph) {
+        // the graph read back the set hash, the table count and the first kGraphLevels level counts
+        const uint32_t head = std::min(c.nlevels, kGraphLevels);
+        memcpy(r->level_counts, ex->h_levels, sizeof(uint64_t) * head);
+        if (c.nlevels > head)
+            GPX_CUDA(cudaMemcpy(r->level_counts + head, ex->d_levels + head, sizeof(uint64_t) * (c.nlevels - head),
+                                cudaMemcpyDeviceToHost));
+        r->set_hash = ex->h_scalar[0];
+        r->table_count = ex->h_scalar[1];
+        r->d2h_bytes = sizeof(Ctrl) + 16 + (uint64_t)kGraphLevels * 8 +
+                       (c.nlevels > head ? (uint64_t)(c.nlevels - head) * 8 : 0);
+    } else {
+        GPX_CUDA(cudaMemcpyAsync(r->level_counts, ex->d_levels, sizeof(uint64_t) * c.nlevels, cudaMemcpyDeviceToHost,
+                                 ex->st));
+        // set hash over the visited states
+        GPX_CUDA(cudaMemsetAsync(ex->d_scalar, 0, 16, ex->st));
         int blocks = (int)std::min<unsigned long long>((count + 255) / 256, 4096);
-        blocks = std::max(blocks, 1);
-        if (ex->kind == 0)
-            set_hash_kernel<K32><<<blocks, 256, 0, ex->st>>>((const K32 *)ex->d_store, count, r->key_words,
-                                                             ex->d_scalar);
-        else if (ex->kind == 1)
-            set_hash_kernel<K64><<<blocks, 256, 0, ex->st>>>((const K64 *)ex->d_store, count, r->key_words,
-                                                             ex->d_scalar);
-        else
-            set_hash_kernel<K128><<<blocks, 256, 0, ex->st>>>((const K128 *)ex->d_store, count, r->key_words,
-                                                              ex->d_scalar);
-        if (ex->o.collect_states || ex->o.verbosity >= 2) {
-            int cb = (int)std::min<unsigned long long>((ex->slots + 255) / 256, 8192);
-            if (ex->kind == 0)
-                count_kernel<K32><<<cb, 256, 0, ex->st>>>((const K32 *)ex->d_table, ex->slots, ex->d_scalar + 1);
-            else if (ex->kind == 1)
-                count_kernel<K64><<<cb, 256, 0, ex->st>>>((const K64 *)ex->d_table, ex->slots, ex->d_scalar + 1);
-            else
-                count_kernel<K128><<<cb, 256, 0, ex->st>>>((const K128 *)ex->d_table, ex->slots, ex->d_scalar + 1);
-        }
+        ex->ks.set_hash(ex->st, std::max(blocks, 1), ex->d_store, count, nullptr, 0, r->key_words, ex->d_scalar);
+        if (ex->o.collect_states || ex->o.verbosity >= 2)
+            ex->ks.count(ex->st, count_blocks(ex), ex->d_table, ex->slots, ex->d_scalar + 1);
         GPX_CUDA(cudaGetLastError());
         unsigned long long h[2] = {0, 0};
         GPX_CUDA(cudaMemcpyAsync(h, ex->d_scalar, 16, cudaMemcpyDeviceToHost, ex->st));
         GPX_CUDA(cudaStreamSynchronize(ex->st));
         r->set_hash = h[0];
         r->table_count = h[1];
+        r->h2d_bytes = (launches - 1) * 2 * sizeof(unsigned int); // -k rearm between launches
+        r->d2h_bytes = launches * sizeof(Ctrl) + (uint64_t)c.nlevels * 8 + 16;
     }
     if (ex->o.collect_states) {
         std::vector<uint32_t> w;
@@ -999,8 +1227,8 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
 
     // carve the array
     const size_t total = GPX_NOALLOC_SCRATCH_BYTES;
-    const size_t off_ctrl = 0, off_scalar = 256, off_levels = 4096;
-    static_assert(sizeof(Ctrl) <= 256, "the control block must fit below the scalar slot");
+    const size_t off_ctrl = 0, off_scalar = 1024, off_levels = 4096;
+    static_assert(sizeof(Ctrl) <= 1024, "the control block must fit below the scalar slot");
     const size_t off_model = round_up(off_levels + (size_t)kMaxLevels * 8, 256);
     const size_t model_bytes = model->dec.words.size() * 4;
     const size_t off_table = round_up(off_model + model_bytes, 256);
@@ -1069,20 +1297,14 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     P.levels_per_launch = opts->kernel_iters > 0 ? (uint32_t)opts->kernel_iters : 0;
     P.total_warps = (uint32_t)(blocks * (threads / 32));
 
-    // clear what must start at zero (the array keeps the previous call's contents)
+    // clear what must start at zero (the array keeps the previous call's contents;
+    // init_kernel resets the control block)
     cudaStream_t st = 0;
     Ctrl c;
-    memset(&c, 0, sizeof c);
-    c.store_count = 1;
-    c.hi = 1;
-    c.nlevels = 1;
-    c.claim = 1;
-    c.phase = mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND;
     GPX_CUDA(cudaMemcpyAsync(base + off_model, model->dec.words.data(), model_bytes, cudaMemcpyHostToDevice, st));
     GPX_CUDA(cudaMemsetAsync(P.table, 0, tb, st));
     GPX_CUDA(cudaMemsetAsync(d_scalar, 0, 64, st));
-    GPX_CUDA(cudaMemcpyAsync(d_ctrl, &c, sizeof c, cudaMemcpyHostToDevice, st));
-    ks.init<<<1, 32, 0, st>>>(P);
+    ks.init<<<1, 32, 0, st>>>(P, mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND);
     GPX_CUDA(cudaGetLastError());
     GPX_CUDA(cudaStreamSynchronize(st));
     auto t_kernels = std::chrono::steady_clock::now();
@@ -1102,12 +1324,7 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     auto t_end = std::chrono::steady_clock::now();
     unsigned long long count = std::min<unsigned long long>(c.store_count, cap);
     int hb = (int)std::max<unsigned long long>(1, std::min<unsigned long long>((count + 255) / 256, 4096));
-    if (kind == 0)
-        set_hash_kernel<K32><<<hb, 256, 0, st>>>((const K32 *)P.store, count, model->dec.key_words, d_scalar);
-    else if (kind == 1)
-        set_hash_kernel<K64><<<hb, 256, 0, st>>>((const K64 *)P.store, count, model->dec.key_words, d_scalar);
-    else
-        set_hash_kernel<K128><<<hb, 256, 0, st>>>((const K128 *)P.store, count, model->dec.key_words, d_scalar);
+    ks.set_hash(st, hb, P.store, count, nullptr, 0, model->dec.key_words, d_scalar);
     GPX_CUDA(cudaGetLastError());
     unsigned long long h = 0;
     GPX_CUDA(cudaMemcpyAsync(&h, d_scalar, sizeof h, cudaMemcpyDeviceToHost, st));

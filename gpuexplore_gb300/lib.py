@@ -71,6 +71,7 @@ class Options(C.Structure):
         ("por", C.c_int32), ("cycle_proviso", C.c_int32), ("property", C.c_int32), ("device", C.c_int32),
         ("seed", C.c_uint64), ("max_states", C.c_uint64), ("store_states", C.c_uint64),
         ("collect_states", C.c_int32), ("bucket_bytes", C.c_int32),
+        ("launch_graph", C.c_int32),
     ]
 
 
@@ -84,6 +85,7 @@ class Result(C.Structure):
         ("expanded", C.c_uint64), ("kernel_ms", C.c_double), ("states_buf", C.POINTER(C.c_uint32)),
         ("table_slots", C.c_uint64), ("slot_bytes", C.c_uint32), ("blocks", C.c_uint32), ("threads", C.c_uint32),
         ("inserts", C.c_uint64), ("evictions", C.c_uint64),
+        ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
     ]
 
 
@@ -262,6 +264,7 @@ def _result_dict(r: Result) -> Dict:
         "verdict": VERDICTS.get(int(r.verdict), str(r.verdict)), "states": int(r.states), "levels": levels,
         "transitions": int(r.transitions), "probes": int(r.probes), "lookups": int(r.lookups),
         "inserts": int(r.inserts), "evictions": int(r.evictions),
+        "h2d_bytes": int(r.h2d_bytes), "d2h_bytes": int(r.d2h_bytes),
         "expanded": int(r.expanded), "launches": int(r.launches), "explore_ms": float(r.explore_ms),
         "kernel_ms": float(r.kernel_ms), "setup_ms": float(r.setup_ms), "set_hash": f"{r.set_hash:016x}",
         "key_words": int(r.key_words), "table_count": int(r.table_count), "table_slots": int(r.table_slots),

@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define GPX_ABI_VERSION 1
+#define GPX_ABI_VERSION 2
 
 /* Status codes.  They replace the reference's exit(1) paths. */
 typedef enum {
@@ -71,7 +71,10 @@ typedef struct {
     uint64_t max_states;    /* stop at the end of the level that reaches this many states (0 = off) */
     uint64_t store_states;  /* capacity of the state store in states (0 = as many as table slots) */
     int32_t collect_states; /* copy the visited states back into gpx_result.states */
-    int32_t bucket_bytes;   /* hash bucket size: 32 (one DRAM sector) or 64; 0 = automatic */
+    int32_t bucket_bytes;   /* hash bucket size in bytes: 0 or 32 (one DRAM sector; other values are rejected) */
+    int32_t launch_graph;   /* 1 (gpx_options_init): with verbosity 0, a run is one CUDA graph -- reset, init,
+                               a device-side loop over the exploration launches (the -k relaunch loop),
+                               set hash and read-back -- built once and replayed; 0: host-driven launches */
 } gpx_options;
 
 /* Result of one exploration.  Arrays are owned by the library: gpx_result_free. */
@@ -101,6 +104,8 @@ typedef struct {
     uint32_t blocks, threads;/* launch configuration that ran */
     uint64_t inserts;        /* states inserted into the hash table by the exploration kernels */
     uint64_t evictions;      /* stored states displaced within their probe sequence to make room */
+    uint64_t h2d_bytes;      /* bytes this run copied host -> device (model uploads are counted by set_model) */
+    uint64_t d2h_bytes;      /* bytes this run copied device -> host (without collect_states / -v output) */
 } gpx_result;
 
 typedef struct gpx_model gpx_model;
