@@ -43,7 +43,7 @@ BUDGET = 100_000_000
 Q_WORDS = 5_000_000_000
 CPU_SAMPLE_BUDGET = 10_000_000  # stops after BFS level 8 (about 4.2e7 states)
 WORKLOAD = "config-2 random gpf network (16 procs + monitor, seed 2024), -d, BFS to 1e8-state budget"
-KERNEL_BUILD = "converged-materialise-v2-fetch32"  # names the kernel version a committed traffic capture belongs to
+KERNEL_BUILD = "static-claims-v3-fetch32"  # names the kernel version a committed traffic capture belongs to
 
 
 def measured_peaks():
@@ -285,6 +285,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpx", choices=["gpx", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="launch the exploration kernels from the host loop instead of one CUDA graph per run "
+                         "(same kernels; used for the ncu captures)")
     ap.add_argument("--budget", type=int, default=BUDGET,
                     help="state budget (smaller values give the profiling cases of the same network)")
     ap.add_argument("--q-words", type=int, default=Q_WORDS, help="hash table size in 32-bit words")
@@ -323,7 +326,7 @@ def main():
     sv_nints = (net.firstbit()[-1] + 1 + 31) // 32  # the reference's words per vector
     model = lib.Model.from_words(words)
     opts = lib.options(property="deadlock", q_words=args.q_words, max_states=args.budget,
-                       store_states=args.store_states, device=local)
+                       store_states=args.store_states, device=local, launch_graph=0 if args.no_graph else 1)
     ex = lib.Explorer(model, opts)
 
     def barrier():
@@ -398,7 +401,7 @@ def main():
                                               "the probe's load instruction"}},
         "clocks": clk,
         # per run: init, the exploration launches, one relaunch test after each, set hash
-        "gpu_launches": sum(2 * x["launches"] + 2 for x in results),
+        "gpu_launches": sum((2 if not args.no_graph else 1) * x["launches"] + 2 for x in results),
         "hash_probe_gbs": 32 * r["probes"] / (kms / 1000.0) / 1e9,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
