@@ -57,7 +57,10 @@ struct BGlobal {
     unsigned int done_count;
     unsigned int error;
     unsigned long long start_ns;
+    unsigned long long launches; // batch_kernel launches of this admission round
 };
+
+constexpr unsigned long long kMaxBatchLaunches = 1ull << 24;
 
 struct BParams {
     BInst *inst;
@@ -238,6 +241,20 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(BParams BP) {
     }
 }
 
+// After each batch_kernel launch of the captured loop: another launch follows
+// while instances remain and no error was recorded (each launch makes progress:
+// every warp claims until its claim budget is spent or nothing is left).
+__global__ void batch_relaunch_kernel(BGlobal *g, uint32_t count, cudaGraphConditionalHandle loop) {
+    unsigned int more = g->done_count < count && !g->error;
+    g->launches++;
+    if (more && g->launches >= kMaxBatchLaunches) {
+        atomicCAS(&g->error, 0u, (unsigned int)GPX_ERR_UNSUPPORTED);
+        more = 0;
+    }
+    __threadfence();
+    cudaGraphSetConditional(loop, more);
+}
+
 // Initial state of every instance (GPUexplore.cu:668-682) and the launch clock.
 __global__ void batch_init_kernel(BParams BP, int first_launch) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -314,7 +331,73 @@ uint64_t estimate_capacity(const gpx_model *m, const gpx_batch_job &j) {
     return (uint64_t)est;
 }
 
-// One launch (plus -k relaunches) over `idx` instances with the given capacities.
+// Record init -> while (instances left) { batch_kernel; batch_relaunch_kernel } -> set hashes.
+cudaError_t capture_batch(cudaStream_t st, BParams BP, int blocks, int threads, size_t smem, cudaEvent_t ev0,
+                          cudaEvent_t ev1, uint32_t count, const BInst *d_inst, const uint32_t *d_words,
+                          unsigned long long *d_hash, cudaGraph_t *out) {
+    cudaStream_t sb = nullptr;
+    bool body_open = false;
+    cudaError_t e = cudaStreamCreateWithFlags(&sb, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+    auto record = [&]() -> cudaError_t {
+        cudaError_t r;
+#define GPX_BCAP(call)                                                                                        \
+    do {                                                                                                      \
+        if ((r = (call)) != cudaSuccess) return r;                                                            \
+    } while (0)
+        GPX_BCAP(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        GPX_BCAP(cudaEventRecordWithFlags(ev0, st, cudaEventRecordExternal));
+        batch_init_kernel<<<(count + 127) / 128, 128, 0, st>>>(BP, 1);
+        GPX_BCAP(cudaGetLastError());
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t *deps = nullptr;
+        const cudaGraphEdgeData *edges = nullptr;
+        size_t ndeps = 0;
+        GPX_BCAP(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &edges, &ndeps));
+        cudaGraphConditionalHandle loop;
+        GPX_BCAP(cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams np = {cudaGraphNodeTypeConditional}; // the rest zero-initialised
+        np.conditional.handle = loop;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        GPX_BCAP(cudaGraphAddNode(&node, g, deps, edges, ndeps, &np));
+        GPX_BCAP(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        GPX_BCAP(cudaStreamBeginCaptureToGraph(sb, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal));
+        body_open = true;
+        void *args[] = {&BP};
+        GPX_BCAP(cudaLaunchKernel((const void *)batch_kernel, dim3(blocks), dim3(threads), args, smem, sb));
+        batch_relaunch_kernel<<<1, 1, 0, sb>>>(BP.g, count, loop);
+        GPX_BCAP(cudaGetLastError());
+        cudaGraph_t body = nullptr; // owned by the conditional node
+        body_open = false;
+        GPX_BCAP(cudaStreamEndCapture(sb, &body));
+        GPX_BCAP(cudaEventRecordWithFlags(ev1, st, cudaEventRecordExternal));
+        batch_hash_kernel<<<std::min<uint32_t>(count, 4096), 256, 0, st>>>(d_inst, count, d_words, d_hash);
+        GPX_BCAP(cudaGetLastError());
+#undef GPX_BCAP
+        return cudaStreamEndCapture(st, out);
+    };
+    e = record();
+    if (e != cudaSuccess) {
+        cudaGraph_t t = nullptr;
+        if (body_open) cudaStreamEndCapture(sb, &t);
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+            t = nullptr;
+            cudaStreamEndCapture(st, &t);
+            if (t) cudaGraphDestroy(t);
+        }
+        cudaGetLastError();
+    }
+    cudaStreamDestroy(sb);
+    return e;
+}
+
+// One admission round: a graph with the batch_kernel launch loop over `idx`
+// instances with the given capacities.
 int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, uint64_t seed,
                const gpx_model *const *models, const gpx_batch_job *jobs, const std::vector<uint32_t> &idx,
                const std::vector<uint64_t> &cap, const gpx_por_model *d_por, std::vector<Outcome> *out,
@@ -360,11 +443,13 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
     BInst *d_inst = nullptr;
     BGlobal *d_g = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaStream_t st = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
     std::vector<uint32_t> hm(model_words, 0);
     BParams BP;
     size_t smem = 0;
     int blocks = 0;
-    void *args[] = {&BP};
     std::vector<unsigned long long> hh(count, 0);
     std::vector<uint64_t> hl;
     for (uint32_t k = 0; k < count; k++) {
@@ -412,28 +497,31 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
     BP.total_warps = (uint32_t)(blocks * (cfg.threads / 32));
     BCUDA(cudaEventCreate(&ev0));
     BCUDA(cudaEventCreate(&ev1));
-    BCUDA(cudaEventRecord(ev0));
-    batch_init_kernel<<<(count + 127) / 128, 128>>>(BP, 1);
-    BCUDA(cudaGetLastError());
-    for (;;) {
-        BCUDA(cudaLaunchKernel((const void *)batch_kernel, dim3(blocks), dim3(cfg.threads), args, smem, 0));
-        (*launches)++;
-        BGlobal g;
-        BCUDA(cudaMemcpy(&g, d_g, sizeof g, cudaMemcpyDeviceToHost));
-        if (g.done_count >= count || g.error) {
-            if (g.error) rc = (int)g.error;
-            break;
+    BCUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    // One graph: init, a device-side while loop over batch_kernel launches
+    // (batch_relaunch_kernel decides whether another follows), set hashes.
+    {
+        cudaError_t ce = capture_batch(st, BP, blocks, cfg.threads, smem, ev0, ev1, count, d_inst, d_words, d_hash,
+                                       &graph);
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
+        if (ce != cudaSuccess) {
+            fprintf(stderr, "gpx batch: building the launch graph failed: %s\n", cudaGetErrorString(ce));
+            cudaGetLastError();
+            rc = GPX_ERR_CUDA;
+            goto done;
         }
     }
-    BCUDA(cudaEventRecord(ev1));
-    BCUDA(cudaEventSynchronize(ev1));
+    BCUDA(cudaGraphLaunch(exec, st));
+    BCUDA(cudaStreamSynchronize(st));
     {
         float ms = 0;
         cudaEventElapsedTime(&ms, ev0, ev1);
         *device_ms += ms;
+        BGlobal g;
+        BCUDA(cudaMemcpy(&g, d_g, sizeof g, cudaMemcpyDeviceToHost));
+        *launches += (uint32_t)g.launches;
+        if (g.error) rc = (int)g.error;
     }
-    batch_hash_kernel<<<std::min<uint32_t>(count, 4096), 256>>>(d_inst, count, d_words, d_hash);
-    BCUDA(cudaGetLastError());
     BCUDA(cudaMemcpy(h.data(), d_inst, count * sizeof(BInst), cudaMemcpyDeviceToHost));
     BCUDA(cudaMemcpy(hh.data(), d_hash, count * 8, cudaMemcpyDeviceToHost));
     hl.resize((size_t)count * kBatchLevels);
@@ -458,6 +546,9 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
         }
     }
 done:
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (st) cudaStreamDestroy(st);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     cudaFree(d_table);

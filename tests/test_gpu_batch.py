@@ -71,6 +71,9 @@ def test_batch_readmission(gpu, tmp_path):
 def test_batch_launch_shapes_and_autotune(gpu, tmp_path):
     cases = _batch_cases(16, 3)
     _check(gpu, tmp_path, cases, claim=32, threads=128, kernel_iters=8)
+    # 8 warps with a budget of 2 claims per launch: the captured loop relaunches on the device
+    items, stats = _check(gpu, tmp_path, cases, claim=8, threads=64, blocks=4, kernel_iters=2)
+    assert stats["launches"] > 10
     items, stats = _check(gpu, tmp_path, cases, autotune=1)
     assert stats["claim"] in (8, 32, 64, 256) and stats["tune_ms"] > 0
     assert stats["p99_ms"] >= stats["p50_ms"] > 0
