@@ -62,10 +62,10 @@ def build_library(force: bool = False) -> str:
     """Compile libgpx.so and the gpuexplore tool; returns the library path."""
     os.makedirs(LIBDIR, exist_ok=True)
     srcs_cu = [os.path.join(CSRC, "gpx_explore.cu"), os.path.join(CSRC, "gpx_batch.cu"),
-               os.path.join(CSRC, "gpx_por.cu")]
+               os.path.join(CSRC, "gpx_por.cu"), os.path.join(CSRC, "gpx_live.cu")]
     srcs_cpp = [os.path.join(CSRC, "gpx_model.cpp")]
     headers = [os.path.join(INCLUDE, "gpx.h"), os.path.join(CSRC, "gpx_model.h"),
-               os.path.join(CSRC, "gpx_device.cuh")]
+               os.path.join(CSRC, "gpx_device.cuh"), os.path.join(CSRC, "gpx_live.h")]
     cli_src = os.path.join(CSRC, "gpuexplore_main.cpp")
     nvcc = _nvcc()
     if force or _stale(LIB, srcs_cu + srcs_cpp + headers):

@@ -612,7 +612,11 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
     for (uint32_t i = 0; i < count; i++) {
         memset(&items[i], 0, sizeof items[i]);
         if (!models[i] || jobs[i].struct_size != sizeof(gpx_batch_job)) return GPX_ERR_INVALID;
-        if (models[i]->dec.state_bits > (uint32_t)kMaxStateBits) {
+        // an instance too wide for 128-bit slots, or with a liveness property (the
+        // accepting-cycle check runs through gpx_explorer_run only)
+        if (models[i]->dec.state_bits > (uint32_t)kMaxStateBits ||
+            (jobs[i].property == GPX_PROP_SAFETY && models[i]->gpf.liveness == 1) ||
+            jobs[i].property == GPX_PROP_LIVENESS) {
             items[i].status = GPX_ERR_UNSUPPORTED;
             items[i].stopped = GPX_STOP_ERROR;
             continue;

@@ -50,6 +50,7 @@
 #include "gpx_model.h"
 
 #include "gpx_device.cuh"
+#include "gpx_live.h"
 
 namespace gpx {
 
@@ -404,6 +405,7 @@ struct gpx_explorer {
     cudaStream_t st_body = nullptr;          // captures the body of the launch loop
     unsigned long long *h_levels = nullptr;  // pinned: the first kGraphLevels level counts
     unsigned long long *h_scalar = nullptr;  // pinned: set hash, table count
+    LiveScratch live;                        // accepting-cycle check (liveness)
 };
 
 namespace {
@@ -758,6 +760,7 @@ void gpx_model_free(gpx_model *m) { delete m; }
 void gpx_explorer_destroy(gpx_explorer *ex) {
     if (!ex) return;
     destroy_graph(ex);
+    live_free(&ex->live);
     if (ex->st_body) cudaStreamDestroy(ex->st_body);
     if (ex->h_levels) cudaFreeHost(ex->h_levels);
     if (ex->h_scalar) cudaFreeHost(ex->h_scalar);
@@ -791,6 +794,11 @@ int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_exp
     ex->property = opts->property;
     if (ex->property == GPX_PROP_SAFETY && model->gpf.liveness == 1) ex->property = GPX_PROP_LIVENESS;
     ex->mode = opts->por ? (opts->cycle_proviso ? MODE_PROVISO : MODE_POR) : MODE_PLAIN;
+    // the accepting-cycle check needs the full state graph
+    if (ex->property == GPX_PROP_LIVENESS && ex->mode != MODE_PLAIN) {
+        delete ex;
+        return GPX_ERR_UNSUPPORTED;
+    }
     ex->kind = select_kind(model->dec.state_bits);
     ex->ks = ex->kind == 0 ? kernels_for<K32>() : (ex->kind == 1 ? kernels_for<K64>() : kernels_for<K128>());
     ex->bits_statevector = model->gpf.bits_statevector + (opts->por ? 1u : 0u);
@@ -840,6 +848,10 @@ int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_exp
 int gpx_explorer_set_model(gpx_explorer *ex, const gpx_model *model) {
     if (!ex || !model) return GPX_ERR_INVALID;
     if (select_kind(model->dec.state_bits) != ex->kind) return GPX_ERR_INVALID;
+    int property = ex->o.property;
+    if (property == GPX_PROP_SAFETY && model->gpf.liveness == 1) property = GPX_PROP_LIVENESS;
+    if (property == GPX_PROP_LIVENESS && ex->mode != MODE_PLAIN) return GPX_ERR_UNSUPPORTED;
+    ex->property = property;
     ex->model = *model;
     ex->bits_statevector = model->gpf.bits_statevector + (ex->o.por ? 1u : 0u);
     int rc = configure_launch(ex);
@@ -976,6 +988,24 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
         r->table_count = h[1];
         r->h2d_bytes = (launches - 1) * 2 * sizeof(unsigned int); // -k rearm between launches
         r->d2h_bytes = launches * sizeof(Ctrl) + (uint64_t)c.nlevels * 8 + 16;
+    }
+    if (ex->property == GPX_PROP_LIVENESS && r->status == GPX_OK && r->stopped == GPX_STOP_DONE) {
+        // the whole state space is in the table: look for an accepting cycle
+        unsigned long long left = 0, rounds = 0;
+        GPX_CUDA(cudaEventRecord(ex->ev[0], ex->st));
+        int rc = live_check(ex->kind, ex->d_table, ex->nbuckets, ex->slots, count, ex->d_model, ex->o.seed, ex->st,
+                            &ex->live, &left, &rounds);
+        if (rc != GPX_OK) return rc;
+        GPX_CUDA(cudaEventRecord(ex->ev[1], ex->st));
+        GPX_CUDA(cudaEventSynchronize(ex->ev[1]));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ex->ev[0], ex->ev[1]);
+        r->live_ms = ms;
+        r->live_states = left;
+        if (left) {
+            r->verdict = GPX_PROP_LIVENESS;
+            r->stopped = GPX_STOP_VIOLATION;
+        }
     }
     if (ex->o.collect_states) {
         std::vector<uint32_t> w;
@@ -1222,6 +1252,7 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     const int mode = opts->por ? (opts->cycle_proviso ? MODE_PROVISO : MODE_POR) : MODE_PLAIN;
     int property = opts->property;
     if (property == GPX_PROP_SAFETY && model->gpf.liveness == 1) property = GPX_PROP_LIVENESS;
+    if (property == GPX_PROP_LIVENESS) return GPX_ERR_UNSUPPORTED; // the cycle check needs scratch of its own
     const int kind = select_kind(model->dec.state_bits);
     KernelSet ks = kind == 0 ? kernels_for<K32>() : (kind == 1 ? kernels_for<K64>() : kernels_for<K128>());
 

@@ -1,0 +1,375 @@
+// gpx_live.cu -- liveness: accepting-cycle detection on the explored state space.
+//
+// The gpf liveness flag (GPUexplore.cu:1888-1898) is parsed by the reference and
+// never checked.  Here it means: the last process is a Buchi automaton whose
+// local state 1 is accepting, and the property is violated iff a reachable
+// cycle passes through an accepting state.  The check runs after a complete
+// exploration (no POR) on the hash table itself, a state's identity being its
+// slot, with the One-Way-Catch-Them-Young fixpoint (Cerna and Pelanek, 2003):
+//
+//   S := visited states
+//   repeat
+//     S := states of S reachable inside S from accepting states of S
+//     S := S without, repeatedly, the states that have no predecessor in S
+//   until S does not change
+//
+// S is empty iff there is no accepting cycle.  Both steps are frontier
+// sweeps: one thread per frontier state enumerates its successors (the same
+// relation as the exploration kernels: local targets, and for every rule the
+// state's lowest member leads, the product of the members' targets), finds each
+// successor's slot and updates per-slot flags and predecessor counts.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+
+#include "gpx.h"
+#include "gpx_device.cuh"
+#include "gpx_live.h"
+#include "gpx_model.h"
+
+namespace gpx {
+
+constexpr uint32_t kInSet = 1u, kMarked = 2u;
+
+// Slot of a key in a table that no one writes to (the key must be present;
+// ~0 otherwise).
+template <class K>
+__device__ unsigned long long find_slot(const K *table, unsigned long long nb, const K &key, uint64_t h) {
+    constexpr int S = KT<K>::kSlots;
+    for (int i = 0; i < kMaxProbe; i++) {
+        const unsigned long long b = bucket_of(h, i, nb);
+        K s[S];
+        KT<K>::bucket(const_cast<K *>(table) + b * S, s);
+#pragma unroll
+        for (int j = 0; j < S; j++) {
+            if (KT<K>::eq(s[j], key)) return b * S + j;
+            if (KT<K>::empty(s[j])) return ~0ull;
+        }
+    }
+    return ~0ull;
+}
+
+// Every successor of `key` under the full transition relation, in the order
+// of the oracle's enumeration (processes' local targets, then rules).
+template <class K, class F> __device__ void for_each_successor(const MView &M, const K &key, F &&f) {
+    const uint32_t n = M.n;
+    for (uint32_t p = 0; p < n; p++) {
+        uint32_t s;
+        const uint32_t *rec = M.state_rec(key, p, s);
+        const uint32_t d = M.pd(p);
+        for (uint32_t i = 0; i < rec[R_LCNT]; i++) {
+            K v = key;
+            KT<K>::set(v, MView::fb_of(d), MView::bs_of(d), M.ltgt(rec[R_LOFF] + i));
+            f(v);
+        }
+        for (uint32_t j = 0; j < rec[R_RCNT]; j++) {
+            const uint32_t k = M.lrule(rec[R_ROFF] + j);
+            const uint32_t mask = M.rmask(k), a = M.ract(k);
+            const uint32_t *g[kMaxProcs];
+            uint32_t parts[kMaxProcs], idx[kMaxProcs], np = 0;
+            bool ok = true;
+            for (uint32_t q = 0; q < n && ok; q++) {
+                if (!(mask >> q & 1u)) continue;
+                uint32_t sq;
+                const uint32_t *gq = M.group(M.state_rec(key, q, sq), a);
+                if (!gq) {
+                    ok = false;
+                } else {
+                    g[np] = gq;
+                    parts[np] = q;
+                    idx[np] = 0;
+                    np++;
+                }
+            }
+            if (!ok) continue;
+            for (;;) {
+                K v = key;
+                for (uint32_t t = 0; t < np; t++) {
+                    const uint32_t dq = M.pd(parts[t]);
+                    KT<K>::set(v, MView::fb_of(dq), MView::bs_of(dq), M.stgt(g[t][1] + idx[t]));
+                }
+                f(v);
+                uint32_t t = 0;
+                while (t < np && ++idx[t] == g[t][2]) idx[t++] = 0;
+                if (t == np) break;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void push(unsigned long long *front, unsigned long long *n, unsigned long long cap,
+                                     unsigned long long slot, unsigned long long *overflow) {
+    const unsigned long long k = atomicAdd(n, 1ull);
+    if (k < cap)
+        front[k] = slot;
+    else
+        atomicAdd(overflow, 1ull);
+}
+
+// count[0]: |S|, count[1]: frontier size, count[2]: next frontier size, count[3]: overflow / missing slots
+template <class K> __global__ void live_init_kernel(const K *table, unsigned long long slots, uint32_t *flag,
+                                                    uint32_t *indeg, unsigned long long *count) {
+    unsigned long long acc = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const bool occ = !KT<K>::empty(KT<K>::load(table + i));
+        flag[i] = occ ? kInSet : 0u;
+        indeg[i] = 0;
+        acc += occ;
+    }
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&count[0], acc);
+}
+
+// Mark the accepting states of S and put them in the frontier.
+template <class K>
+__global__ void live_seed_kernel(const K *table, unsigned long long slots, const uint32_t *model, uint32_t *flag,
+                                 unsigned long long *front, unsigned long long cap, unsigned long long *count) {
+    MView M;
+    M.init(model);
+    const uint32_t d = M.pd(M.n - 1);
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        if (!(flag[i] & kInSet)) continue;
+        if (KT<K>::get(KT<K>::load(table + i), MView::fb_of(d), MView::bs_of(d)) != 1) continue;
+        flag[i] |= kMarked;
+        push(front, &count[1], cap, i, &count[3]);
+    }
+}
+
+// One forward round: mark the unmarked successors in S of the frontier.
+template <class K>
+__global__ void live_reach_kernel(const K *table, unsigned long long nb, const uint32_t *model, unsigned long long seed,
+                                  uint32_t *flag, const unsigned long long *front, unsigned long long nfront,
+                                  unsigned long long *next, unsigned long long cap, unsigned long long *count) {
+    MView M;
+    M.init(model);
+    for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; t < nfront;
+         t += (unsigned long long)gridDim.x * blockDim.x) {
+        const K key = KT<K>::load(table + front[t]);
+        for_each_successor(M, key, [&](const K &v) {
+            const unsigned long long j = find_slot(table, nb, v, KT<K>::hash(v, seed));
+            if (j == ~0ull) {
+                atomicAdd(&count[3], 1ull);
+                return;
+            }
+            if ((flag[j] & kInSet) && !(atomicOr(&flag[j], kMarked) & kMarked)) push(next, &count[2], cap, j, &count[3]);
+        });
+    }
+}
+
+// S := marked states of S; clears the marks; counts |S|.
+__global__ void live_restrict_kernel(unsigned long long slots, uint32_t *flag, uint32_t *indeg,
+                                     unsigned long long *count) {
+    unsigned long long acc = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t f = flag[i];
+        const uint32_t keep = (f & kInSet) && (f & kMarked) ? kInSet : 0u;
+        flag[i] = keep;
+        indeg[i] = 0;
+        acc += keep;
+    }
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&count[0], acc);
+}
+
+// Predecessor counts inside S (edges counted with multiplicity).
+template <class K>
+__global__ void live_indeg_kernel(const K *table, unsigned long long nb, unsigned long long slots,
+                                  const uint32_t *model, unsigned long long seed, const uint32_t *flag,
+                                  uint32_t *indeg, unsigned long long *count) {
+    MView M;
+    M.init(model);
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        if (!(flag[i] & kInSet)) continue;
+        const K key = KT<K>::load(table + i);
+        for_each_successor(M, key, [&](const K &v) {
+            const unsigned long long j = find_slot(table, nb, v, KT<K>::hash(v, seed));
+            if (j == ~0ull) {
+                atomicAdd(&count[3], 1ull);
+                return;
+            }
+            if (flag[j] & kInSet) atomicAdd(&indeg[j], 1u);
+        });
+    }
+}
+
+// The states of S without predecessors in S start the peeling.
+__global__ void live_sources_kernel(unsigned long long slots, const uint32_t *flag, const uint32_t *indeg,
+                                    unsigned long long *front, unsigned long long cap, unsigned long long *count) {
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        if ((flag[i] & kInSet) && indeg[i] == 0) push(front, &count[1], cap, i, &count[3]);
+}
+
+// One peeling round: remove the frontier from S; successors whose last
+// predecessor in S went form the next frontier.
+template <class K>
+__global__ void live_peel_kernel(const K *table, unsigned long long nb, const uint32_t *model, unsigned long long seed,
+                                 uint32_t *flag, uint32_t *indeg, const unsigned long long *front,
+                                 unsigned long long nfront, unsigned long long *next, unsigned long long cap,
+                                 unsigned long long *count) {
+    MView M;
+    M.init(model);
+    for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; t < nfront;
+         t += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long i = front[t];
+        flag[i] = 0;
+        const K key = KT<K>::load(table + i);
+        for_each_successor(M, key, [&](const K &v) {
+            const unsigned long long j = find_slot(table, nb, v, KT<K>::hash(v, seed));
+            if (j == ~0ull) {
+                atomicAdd(&count[3], 1ull);
+                return;
+            }
+            if ((flag[j] & kInSet) && atomicSub(&indeg[j], 1u) == 1u) push(next, &count[2], cap, j, &count[3]);
+        });
+    }
+}
+
+__global__ void live_count_kernel(unsigned long long slots, const uint32_t *flag, unsigned long long *count) {
+    unsigned long long acc = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        acc += flag[i] & kInSet;
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&count[0], acc);
+}
+
+void live_free(LiveScratch *s) {
+    cudaFree(s->flag);
+    cudaFree(s->indeg);
+    cudaFree(s->front[0]);
+    cudaFree(s->front[1]);
+    cudaFree(s->count);
+    *s = LiveScratch();
+}
+
+namespace {
+
+#define LCUDA(call)                                                                                           \
+    do {                                                                                                      \
+        cudaError_t _e = (call);                                                                              \
+        if (_e != cudaSuccess) {                                                                              \
+            fprintf(stderr, "gpx liveness: %s failed: %s\n", #call, cudaGetErrorString(_e));               \
+            return (_e == cudaErrorMemoryAllocation) ? GPX_ERR_NOMEM : GPX_ERR_CUDA;                          \
+        }                                                                                                     \
+    } while (0)
+
+int grid_for(unsigned long long n) {
+    unsigned long long b = (n + 255) / 256;
+    return (int)(b < 1 ? 1 : (b > 8192 ? 8192 : b));
+}
+
+template <class K>
+int run(const K *table, unsigned long long nb, unsigned long long slots, unsigned long long states,
+        const uint32_t *model, unsigned long long seed, cudaStream_t st, LiveScratch *s,
+        unsigned long long *set_states, unsigned long long *rounds) {
+    if (s->slots < slots) {
+        cudaFree(s->flag);
+        cudaFree(s->indeg);
+        s->flag = nullptr;
+        s->indeg = nullptr;
+        LCUDA(cudaMalloc(&s->flag, slots * 4));
+        LCUDA(cudaMalloc(&s->indeg, slots * 4));
+        s->slots = slots;
+    }
+    if (s->front_cap < states) {
+        for (auto &f : s->front) {
+            cudaFree(f);
+            f = nullptr;
+            LCUDA(cudaMalloc(&f, states * 8));
+        }
+        s->front_cap = states;
+    }
+    if (!s->count) LCUDA(cudaMalloc(&s->count, 4 * 8));
+    unsigned long long h[4];
+    auto read = [&]() -> int {
+        LCUDA(cudaMemcpyAsync(h, s->count, sizeof h, cudaMemcpyDeviceToHost, st));
+        LCUDA(cudaStreamSynchronize(st));
+        if (h[3]) {
+            fprintf(stderr, "gpx liveness: %llu successors missing from the table or frontier overflow\n", h[3]);
+            return GPX_ERR_INVALID;
+        }
+        return GPX_OK;
+    };
+    const int gs = grid_for(slots);
+    *rounds = 0;
+    LCUDA(cudaMemsetAsync(s->count, 0, sizeof h, st));
+    live_init_kernel<K><<<gs, 256, 0, st>>>(table, slots, s->flag, s->indeg, s->count);
+    LCUDA(cudaGetLastError());
+    int rc = read();
+    if (rc) return rc;
+    unsigned long long size = h[0];
+    for (;;) {
+        const unsigned long long before = size;
+        // forward closure from the accepting states of S
+        LCUDA(cudaMemsetAsync(s->count, 0, sizeof h, st));
+        live_seed_kernel<K><<<gs, 256, 0, st>>>(table, slots, model, s->flag, s->front[0], s->front_cap, s->count);
+        LCUDA(cudaGetLastError());
+        if ((rc = read())) return rc;
+        int cur = 0;
+        unsigned long long nfront = h[1];
+        while (nfront) {
+            LCUDA(cudaMemsetAsync(s->count + 2, 0, 8, st));
+            live_reach_kernel<K><<<grid_for(nfront), 256, 0, st>>>(table, nb, model, seed, s->flag, s->front[cur],
+                                                                   nfront, s->front[cur ^ 1], s->front_cap, s->count);
+            LCUDA(cudaGetLastError());
+            if ((rc = read())) return rc;
+            nfront = h[2];
+            cur ^= 1;
+            ++*rounds;
+        }
+        LCUDA(cudaMemsetAsync(s->count, 0, sizeof h, st));
+        live_restrict_kernel<<<gs, 256, 0, st>>>(slots, s->flag, s->indeg, s->count);
+        LCUDA(cudaGetLastError());
+        if ((rc = read())) return rc;
+        size = h[0];
+        if (size == 0) break;
+        // peel the states with no predecessor in S
+        LCUDA(cudaMemsetAsync(s->count, 0, sizeof h, st));
+        live_indeg_kernel<K><<<gs, 256, 0, st>>>(table, nb, slots, model, seed, s->flag, s->indeg, s->count);
+        LCUDA(cudaGetLastError());
+        live_sources_kernel<<<gs, 256, 0, st>>>(slots, s->flag, s->indeg, s->front[0], s->front_cap, s->count);
+        LCUDA(cudaGetLastError());
+        if ((rc = read())) return rc;
+        cur = 0;
+        nfront = h[1];
+        while (nfront) {
+            LCUDA(cudaMemsetAsync(s->count + 2, 0, 8, st));
+            live_peel_kernel<K><<<grid_for(nfront), 256, 0, st>>>(table, nb, model, seed, s->flag, s->indeg,
+                                                                  s->front[cur], nfront, s->front[cur ^ 1],
+                                                                  s->front_cap, s->count);
+            LCUDA(cudaGetLastError());
+            if ((rc = read())) return rc;
+            nfront = h[2];
+            cur ^= 1;
+            ++*rounds;
+        }
+        LCUDA(cudaMemsetAsync(s->count, 0, sizeof h, st));
+        live_count_kernel<<<gs, 256, 0, st>>>(slots, s->flag, s->count);
+        LCUDA(cudaGetLastError());
+        if ((rc = read())) return rc;
+        size = h[0];
+        if (size == 0 || size == before) break;
+    }
+    *set_states = size;
+    return GPX_OK;
+}
+
+} // namespace
+
+int live_check(int kind, void *table, unsigned long long nbuckets, unsigned long long slots,
+               unsigned long long states, const uint32_t *model, unsigned long long seed, cudaStream_t st,
+               LiveScratch *s, unsigned long long *set_states, unsigned long long *rounds) {
+    if (kind == 0)
+        return run<K32>((const K32 *)table, nbuckets, slots, states, model, seed, st, s, set_states, rounds);
+    if (kind == 1)
+        return run<K64>((const K64 *)table, nbuckets, slots, states, model, seed, st, s, set_states, rounds);
+    return run<K128>((const K128 *)table, nbuckets, slots, states, model, seed, st, s, set_states, rounds);
+}
+
+} // namespace gpx

@@ -133,6 +133,101 @@ def add_safety_monitor(net: Network, i: int, a: int, j: int, b: int) -> Network:
     return out
 
 
+def add_liveness_monitor(net: Network, i: int, a: int) -> Network:
+    """Embed the liveness property "process i takes a transition into local state
+    a infinitely often" as a Buchi monitor for its negation, appended last, and
+    set the gpf liveness flag.
+
+    Accepting state 1 (the convention the safety monitor uses for its error
+    state): monitor state 0 may guess, by a local tau, that no such transition
+    follows any more and move to 1; in 1 a transition of i into a traps the
+    monitor in state 2.  Every local transition of i into a becomes a two-party
+    synchronisation with the monitor, enabled in all three monitor states, so
+    the monitor never blocks the network.  A violation is a reachable cycle
+    through a state with the monitor in 1: a run on which i eventually never
+    enters a again.  Requires that no synchronising transition of i targets a.
+    """
+    n = net.nprocs
+    M = n
+    E = net.nactions()
+    for s in range(net.nstates[i]):
+        for ts in net.sync[i][s].values():
+            if a in ts:
+                raise ValueError("a synchronising transition of i targets a")
+    out = Network(
+        nstates=net.nstates + [3],
+        local=[[list(ts) for ts in net.local[p]] for p in range(n)] + [[[1], [], []]],
+        sync=[[dict((k, list(v)) for k, v in d.items()) for d in net.sync[p]] for p in range(n)]
+        + [[{} for _ in range(3)]],
+        rules=dict((k, list(v)) for k, v in net.rules.items()),
+        liveness=1,
+    )
+    for s in range(out.nstates[i]):
+        keep = []
+        for t in out.local[i][s]:
+            if t == a:
+                _add_sync(out, i, s, E, t)
+            else:
+                keep.append(t)
+        out.local[i][s] = keep
+    out.rules[E] = [(1 << i) | (1 << M)]
+    for s, t in ((0, 0), (1, 2), (2, 2)):
+        _add_sync(out, M, s, E, t)
+    return out
+
+
+def liveness_network(seed: int, nprocs: int = 6, states: Tuple[int, int] = (3, 6),
+                     outdeg: Tuple[int, int] = (1, 2), sync_frac: float = 0.3) -> Network:
+    """A random network (no safety monitor) with a liveness monitor over a seeded
+    (process, local state) pair that no synchronising transition targets."""
+    rng = random.Random(seed * 7919 + 13)
+    for attempt in range(64):
+        net = random_network(seed * 1000 + attempt, nprocs=nprocs, states=states, outdeg=outdeg,
+                             sync_frac=sync_frac, safety=False)
+        pairs = [(i, a) for i in range(nprocs) for a in range(net.nstates[i])
+                 if not any(a in ts for st in net.sync[i] for ts in st.values())
+                 and any(a in ts for ts in net.local[i])]
+        if pairs:
+            i, a = rng.choice(pairs)
+            return add_liveness_monitor(net, i, a)
+    raise ValueError("no eligible (process, state) pair")
+
+
+def progress_network(seed: int, nprocs: int = 5, states: Tuple[int, int] = (3, 6), cyclic: bool = False,
+                     sync_frac: float = 0.4) -> Network:
+    """A network whose liveness verdict is known by construction, with the
+    monitor of :func:`add_liveness_monitor` for "process 0 takes a transition
+    into local state 0 infinitely often".  Process 0 moves forward (s -> t > s)
+    plus one closing edge back to 0; processes 1.. move forward only, locally or
+    synchronising in pairs.  Every cycle then runs through process 0's closing
+    edge: the property holds.  With `cyclic`, process 1 gets a backward edge,
+    so a cycle avoiding process 0 exists: a violation (when reachable)."""
+    rng = random.Random(seed)
+    nst = [rng.randint(states[0], states[1]) for _ in range(nprocs)]
+    net = _empty(nst)
+    k = nst[0]
+    for s in range(k - 1):
+        for t in sorted(set(rng.sample(range(s + 1, k), min(2, k - 1 - s)))):
+            _add_local(net, 0, s, t)
+    _add_local(net, 0, k - 1, 0)
+    others = list(range(1, nprocs))
+    rules, acts_of = _sync_pool(rng, others, 2 * len(others), (2, 2))
+    net.rules = rules
+    for p in others:
+        for s in range(nst[p] - 1):
+            for _ in range(rng.randint(1, 2)):
+                t = rng.randrange(s + 1, nst[p])
+                if acts_of[p - 1] and rng.random() < sync_frac:
+                    _add_sync(net, p, s, rng.choice(acts_of[p - 1]), t)
+                else:
+                    _add_local(net, p, s, t)
+    if cyclic:
+        _add_local(net, 1, nst[1] - 1, 0)
+        _add_local(net, 1, 0, nst[1] - 1)
+    _prune_unused_rules(net)
+    return add_liveness_monitor(net, 0, 0)
+
+
 def _sync_pool(rng: random.Random, procs: List[int], nactions: int,
                parties: Tuple[int, int], groups: Optional[List[List[int]]] = None,
                p_subrule: float = 0.25) -> Tuple[Dict[int, List[int]], List[List[int]]]:

@@ -15,6 +15,7 @@ import numpy as np
 from .build import LIB
 
 GPX_OK = 0
+GPX_ERR_UNSUPPORTED = 7
 STATUS = ["ok", "parse", "no_gpu", "cuda", "table_full", "timeout", "invalid", "unsupported", "store_full", "nomem"]
 PROP_NONE, PROP_DEADLOCK, PROP_SAFETY, PROP_LIVENESS = 0, 1, 2, 3
 PROPERTIES = {"none": PROP_NONE, "deadlock": PROP_DEADLOCK, "safety": PROP_SAFETY, "liveness": PROP_LIVENESS}
@@ -85,7 +86,7 @@ class Result(C.Structure):
         ("expanded", C.c_uint64), ("kernel_ms", C.c_double), ("states_buf", C.POINTER(C.c_uint32)),
         ("table_slots", C.c_uint64), ("slot_bytes", C.c_uint32), ("blocks", C.c_uint32), ("threads", C.c_uint32),
         ("inserts", C.c_uint64), ("evictions", C.c_uint64),
-        ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
+        ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("live_states", C.c_uint64), ("live_ms", C.c_double),
     ]
 
 
@@ -264,7 +265,8 @@ def _result_dict(r: Result) -> Dict:
         "verdict": VERDICTS.get(int(r.verdict), str(r.verdict)), "states": int(r.states), "levels": levels,
         "transitions": int(r.transitions), "probes": int(r.probes), "lookups": int(r.lookups),
         "inserts": int(r.inserts), "evictions": int(r.evictions),
-        "h2d_bytes": int(r.h2d_bytes), "d2h_bytes": int(r.d2h_bytes),
+        "h2d_bytes": int(r.h2d_bytes), "d2h_bytes": int(r.d2h_bytes), "live_states": int(r.live_states),
+        "live_ms": float(r.live_ms),
         "expanded": int(r.expanded), "launches": int(r.launches), "explore_ms": float(r.explore_ms),
         "kernel_ms": float(r.kernel_ms), "setup_ms": float(r.setup_ms), "set_hash": f"{r.set_hash:016x}",
         "key_words": int(r.key_words), "table_count": int(r.table_count), "table_slots": int(r.table_slots),

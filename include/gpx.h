@@ -106,6 +106,8 @@ typedef struct {
     uint64_t evictions;      /* stored states displaced within their probe sequence to make room */
     uint64_t h2d_bytes;      /* bytes this run copied host -> device (model uploads are counted by set_model) */
     uint64_t d2h_bytes;      /* bytes this run copied device -> host (without collect_states / -v output) */
+    uint64_t live_states;    /* liveness: states left in the accepting-cycle fixpoint (0 = no accepting cycle) */
+    double live_ms;          /* liveness: device time of the accepting-cycle check */
 } gpx_result;
 
 typedef struct gpx_model gpx_model;

@@ -634,7 +634,10 @@ typedef struct {
     int stopped; /* 0 done, 1 violation, 2 budget */
     uint64_t set_hash;
     double seconds;
+    uint64_t live_states; /* states in accepting cyclic components (liveness) */
 } result_t;
+
+static int liveness_check(const gpf_t *m, hset_t *shards, uint32_t S, uint64_t *scc_states);
 
 static double now_s(void) {
     struct timespec ts;
@@ -804,8 +807,152 @@ static int run(const gpf_t *m, const opts_t *o, result_t *res) {
         for (uint64_t i = 0; i < shards[j].cap; i++)
             if (shards[j].used[i]) sh += key_hash(shards[j].keys + i * W, W);
     res->set_hash = sh;
+    res->live_states = 0;
+    if (o->property == PROP_LIVENESS && !o->por && res->stopped == 0 && !res->violation) {
+        if (liveness_check(m, shards, S, &res->live_states)) {
+            res->violation = 1;
+            res->stopped = 1;
+        }
+    }
     if (dump) fclose(dump);
     return 0;
+}
+
+/* --------------------------------------------------------------- liveness */
+
+/* The gpf liveness flag (G:1888-1898) is parsed but never checked by the
+ * reference.  Here it means: the last process is a Buchi automaton whose local
+ * state 1 is accepting, and the property is violated iff some reachable cycle
+ * contains an accepting state.  Checked after a complete exploration without
+ * POR: the explicit graph of the visited set, Tarjan's strongly connected
+ * components (iterative), and a component with an accepting state that holds
+ * a cycle (more than one state, or a self-loop) is a violation. */
+typedef struct {
+    const gpf_t *m;
+    const uint32_t *all;  /* N x W visited states */
+    const int64_t *slot;  /* open-addressing index: slot -> state index or -1 */
+    uint64_t mask;
+    uint32_t *edges;
+    uint64_t nedges, cap;
+} graph_ctx_t;
+
+static int64_t index_of(const graph_ctx_t *g, const uint32_t *k) {
+    const uint32_t W = g->m->W;
+    uint64_t i = key_hash(k, W) & g->mask;
+    for (;;) {
+        int64_t v = g->slot[i];
+        if (v < 0) return -1;
+        if (!memcmp(g->all + (uint64_t)v * W, k, W * 4)) return v;
+        i = (i + 1) & g->mask;
+    }
+}
+
+static void emit_edge(void *ctx, const uint32_t *succ, origin_t o) {
+    (void)o;
+    graph_ctx_t *g = (graph_ctx_t *)ctx;
+    int64_t j = index_of(g, succ);
+    if (j < 0) { /* every successor of a visited state was visited: the search was complete */
+        fprintf(stderr, "ERROR: liveness check: successor outside the visited set\n");
+        exit(1);
+    }
+    if (g->nedges == g->cap) {
+        g->cap = g->cap ? 2 * g->cap : 1024;
+        g->edges = (uint32_t *)realloc(g->edges, g->cap * 4);
+    }
+    g->edges[g->nedges++] = (uint32_t)j;
+}
+
+/* 1 when an accepting cycle exists; *scc_states = states in accepting cyclic components */
+static int liveness_check(const gpf_t *m, hset_t *shards, uint32_t S, uint64_t *scc_states) {
+    const uint32_t W = m->W, n = m->nr_procs;
+    uint64_t N = 0;
+    for (uint32_t j = 0; j < S; j++) N += shards[j].n;
+    if (N >= 0xFFFFFFFFull) capacity_exceeded("states for the liveness check");
+    uint32_t *all = (uint32_t *)malloc(N * W * 4);
+    uint64_t k = 0;
+    for (uint32_t j = 0; j < S; j++)
+        for (uint64_t i = 0; i < shards[j].cap; i++)
+            if (shards[j].used[i]) memcpy(all + (k++) * W, shards[j].keys + i * W, W * 4);
+    uint64_t cap = 1;
+    while (cap < 2 * N) cap <<= 1;
+    int64_t *slot = (int64_t *)malloc(cap * 8);
+    for (uint64_t i = 0; i < cap; i++) slot[i] = -1;
+    for (uint64_t v = 0; v < N; v++) {
+        uint64_t i = key_hash(all + v * W, W) & (cap - 1);
+        while (slot[i] >= 0) i = (i + 1) & (cap - 1);
+        slot[i] = (int64_t)v;
+    }
+    graph_ctx_t g = {m, all, slot, cap - 1, NULL, 0, 0};
+    uint64_t *first = (uint64_t *)malloc((N + 1) * 8);
+    expand_t *x = (expand_t *)malloc(sizeof(expand_t));
+    for (uint64_t v = 0; v < N; v++) {
+        first[v] = g.nedges;
+        collect(m, all + v * W, x);
+        expand_all(m, all + v * W, x, emit_edge, &g);
+    }
+    first[N] = g.nedges;
+    free(x);
+    /* Tarjan, iterative: index/low per state, an explicit DFS stack of (state, next edge) */
+    uint32_t *idx = (uint32_t *)malloc(N * 4), *low = (uint32_t *)malloc(N * 4);
+    uint8_t *on = (uint8_t *)calloc(N, 1);
+    uint32_t *stk = (uint32_t *)malloc(N * 4), *dfs = (uint32_t *)malloc(N * 4);
+    uint64_t *it = (uint64_t *)malloc(N * 8);
+    for (uint64_t v = 0; v < N; v++) idx[v] = 0xFFFFFFFFu;
+    uint32_t counter = 0;
+    uint64_t sp = 0, dp = 0, found = 0;
+    for (uint64_t r = 0; r < N; r++) {
+        if (idx[r] != 0xFFFFFFFFu) continue;
+        dfs[dp++] = (uint32_t)r;
+        idx[r] = low[r] = counter++;
+        it[r] = first[r];
+        stk[sp++] = (uint32_t)r;
+        on[r] = 1;
+        while (dp) {
+            uint32_t v = dfs[dp - 1];
+            if (it[v] < first[v + 1]) {
+                uint32_t w = g.edges[it[v]++];
+                if (idx[w] == 0xFFFFFFFFu) {
+                    idx[w] = low[w] = counter++;
+                    it[w] = first[w];
+                    stk[sp++] = w;
+                    on[w] = 1;
+                    dfs[dp++] = w;
+                } else if (on[w] && idx[w] < low[v]) {
+                    low[v] = idx[w];
+                }
+                continue;
+            }
+            dp--;
+            if (dp && low[v] < low[dfs[dp - 1]]) low[dfs[dp - 1]] = low[v];
+            if (low[v] != idx[v]) continue;
+            /* v roots a component: pop it */
+            uint64_t size = 0, acc = 0, self = 0, top = sp;
+            uint32_t w;
+            do {
+                w = stk[--sp];
+                on[w] = 0;
+                size++;
+                if (get_local(m, all + (uint64_t)w * W, n - 1) == 1) acc = 1;
+            } while (w != v);
+            if (size == 1)
+                for (uint64_t e = first[v]; e < first[v + 1]; e++)
+                    if (g.edges[e] == v) self = 1;
+            if (acc && (size > 1 || self)) found += size;
+            (void)top;
+        }
+    }
+    *scc_states = found;
+    free(all);
+    free(slot);
+    free(first);
+    free(g.edges);
+    free(idx);
+    free(low);
+    free(on);
+    free(stk);
+    free(dfs);
+    free(it);
+    return found > 0;
 }
 
 static void usage(void) {
@@ -875,6 +1022,10 @@ int main(int argc, char **argv) {
         fprintf(stderr, "ERROR: state vector too wide for the oracle\n");
         return 1;
     }
+    if (o.property == PROP_LIVENESS && o.por) {
+        fprintf(stderr, "ERROR: the liveness check needs the full state graph (no --por)\n");
+        return 1;
+    }
     result_t r;
     run(&m, &o, &r);
     int T = 1;
@@ -882,12 +1033,14 @@ int main(int argc, char **argv) {
     T = o.threads > 0 ? o.threads : omp_get_max_threads();
 #endif
     const char *verdict = "none";
-    if (r.violation) verdict = o.property == PROP_DEADLOCK ? "deadlock" : "safety";
+    if (r.violation)
+        verdict = o.property == PROP_DEADLOCK ? "deadlock" : (o.property == PROP_LIVENESS ? "liveness" : "safety");
     printf("{\"states\": %" PRIu64 ", \"levels\": [", r.states);
     for (uint32_t i = 0; i < r.nlevels; i++) printf("%s%" PRIu64, i ? ", " : "", r.level_counts[i]);
     printf("], \"verdict\": \"%s\", \"stopped\": \"%s\", \"generated\": %" PRIu64
-           ", \"set_hash\": \"%016" PRIx64 "\", \"threads\": %d, \"seconds\": %.6f, \"words\": %u}\n",
+           ", \"set_hash\": \"%016" PRIx64 "\", \"threads\": %d, \"seconds\": %.6f, \"words\": %u"
+           ", \"live_states\": %" PRIu64 "}\n",
            verdict, r.stopped == 0 ? "done" : (r.stopped == 1 ? "violation" : "budget"), r.generated,
-           r.set_hash, T, r.seconds, m.W);
+           r.set_hash, T, r.seconds, m.W, r.live_states);
     return 0;
 }

@@ -158,3 +158,37 @@ def set_hash(net: Network, states: Optional[Set[State]]) -> str:
     for s in states or ():
         total = (total + key_hash(pack(net, s))) & MASK64
     return f"{total:016x}"
+
+
+def accepting_cycle(net: Network, max_states: int = 200_000) -> Tuple[int, bool]:
+    """(reachable states, whether a reachable cycle passes through a state whose
+    last process is in local state 1) -- the liveness check, by networkx's
+    strongly connected components over the explicit graph."""
+    import networkx as nx
+
+    init = tuple([0] * net.nprocs)
+    g = nx.DiGraph()
+    g.add_node(init)
+    seen = {init}
+    stack = [init]
+    while stack:
+        s = stack.pop()
+        for v, _ in successors(net, s):
+            g.add_edge(s, v)
+            if v not in seen:
+                seen.add(v)
+                if len(seen) > max_states:
+                    raise ValueError("state space too large for the networkx check")
+                stack.append(v)
+    acc = False
+    for comp in nx.strongly_connected_components(g):
+        if not any(s[-1] == 1 for s in comp):
+            continue
+        if len(comp) > 1:
+            acc = True
+            break
+        (s,) = tuple(comp)
+        if g.has_edge(s, s):
+            acc = True
+            break
+    return len(seen), acc
