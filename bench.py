@@ -207,6 +207,49 @@ def run_other_workload(args, local):
                             **{k: v for k, v in ev.items() if k != "per_seed"}})
         print(json.dumps(line), flush=True)
         return
+    if args.workload == "liveness":
+        # accepting-cycle check: a 20-process network, 5.2M states, where the
+        # property holds (the whole fixpoint runs), and its violating variant
+        import time as _t
+        nets = {"holds": gen.progress_network(7, nprocs=20, states=(3, 4), sync_frac=0.5),
+                "violated": gen.progress_network(7, nprocs=20, states=(3, 4), sync_frac=0.5, cyclic=True)}
+        per = {}
+        for name, net in nets.items():
+            m = lib.Model.from_words(gpf.encode(net))
+            ex = lib.Explorer(m, lib.options(device=local, property="safety", cycle_proviso=1, q_words=1 << 29))
+            for _ in range(args.warmup):
+                ex.run()
+            ker, live, r = [], [], None
+            for _ in range(args.steps):
+                r = ex.run()
+                ker.append(r["kernel_ms"])
+                live.append(r["live_ms"])
+            ex.close()
+            per[name] = {"states": r["states"], "verdict": r["verdict"], "explore_ms": statistics.median(ker),
+                         "check_ms": statistics.median(live), "fixpoint_states": r["live_states"]}
+        h = per["holds"]
+        value = h["states"] / ((h["explore_ms"] + h["check_ms"]) / 1000.0)
+        line.update(metric="states checked/s (exploration + accepting-cycle check)", value=value,
+                    ms_per_step=h["explore_ms"] + h["check_ms"],
+                    config={"workload": "liveness: progress network (20 processes + Buchi monitor, seed 7), "
+                                        "-p on a liveness gpf, full exploration + accepting-cycle check",
+                            **{f"{k}_{kk}": vv for k, v in per.items() for kk, vv in v.items()}})
+        if not args.no_cpu_baseline:
+            from gpuexplore_gb300.build import ORACLE
+            threads = os.cpu_count() or 1
+            with tempfile.TemporaryDirectory() as d:
+                path = os.path.join(d, "live.gpf")
+                gpf.write(nets["holds"], path)
+                t0 = _t.time()
+                o = json.loads(subprocess.run([ORACLE, path, "-p", "--threads", str(threads)], capture_output=True,
+                                              text=True, check=True).stdout)
+                secs = _t.time() - t0
+            line["cpu_baseline"] = {"value": o["states"] / secs, "unit": "states/s", "cores": threads, "kind": "port",
+                                    "sample": f"the whole 'holds' network ({o['states']} states): OpenMP BFS, then "
+                                              "a single-threaded Tarjan SCC check (verdict "
+                                              f"{o['verdict']})"}
+        print(json.dumps(line), flush=True)
+        return
     if args.workload in ("config1", "config3"):
         if args.workload == "config1":
             nets = [gen.ring(s) for s in range(1, 11)]
@@ -292,7 +335,8 @@ def main():
                     help="state budget (smaller values give the profiling cases of the same network)")
     ap.add_argument("--q-words", type=int, default=Q_WORDS, help="hash table size in 32-bit words")
     ap.add_argument("--store-states", type=int, default=0, help="state store capacity (0: table slots)")
-    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3", "config4", "config5"],
+    ap.add_argument("--workload", default="config2",
+                    choices=["config1", "config2", "config3", "config4", "config5", "liveness"],
                     help="config2 is the headline; the others print their own line")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--train-seeds", type=int, default=2000)
