@@ -285,6 +285,23 @@ def run_other_workload(args, local):
                 bms += st["device_ms"]
                 bst += st["states"]
             extra = {"batched_states_per_s": bst / (bms / 1000.0), "batched_ms_per_step": bms / args.steps}
+        else:
+            # the other reductions on the same networks: states kept and device time
+            ex.close()
+            for name, por in (("ample", 3), ("stubborn", 4), ("none", 0)):
+                kwv = dict(kw, por=por)
+                exv = lib.Explorer(models[0], lib.options(device=local, **kwv))
+                vs, vms = 0, 0.0
+                for m in models:
+                    exv.set_model(m)
+                    exv.run()
+                    r = exv.run()
+                    vs += r["states"]
+                    vms += r["setup_ms"] + r["kernel_ms"]
+                exv.close()
+                extra[f"{name}_states"] = vs
+                extra[f"{name}_ms"] = vms
+            extra["note"] = "none_* = unreduced BFS to the same state budget"
         line.update(value=states / (ms / 1000.0), ms_per_step=ms / args.steps,
                     config={"workload": desc, "states_per_step": states // args.steps, "networks": len(nets),
                             "kernel_ms_per_step": kms / args.steps, **extra})

@@ -38,6 +38,8 @@ static const char *kHelp =
     "  --store NUM        Capacity of the state store in states\n"
     "  --device NUM       CUDA device to use\n"
     "  --por-model FILE   Use the learned cluster proposal in FILE (a gpx_por_model) with --por\n"
+    "  --ample            Partial-order reduction with single-process ample sets\n"
+    "  --stubborn         Partial-order reduction with stubborn sets (necessary enabling processes)\n"
     "  -h, --help         Show this help message\n";
 
 static uint64_t mix64(uint64_t z) {
@@ -102,7 +104,13 @@ int main(int argc, char **argv) {
             o.cycle_proviso = 1;
             i += 1;
         } else if (!strcmp(a, "--por")) {
-            o.por = 1;
+            if (!o.por) o.por = 1;
+            i += 1;
+        } else if (!strcmp(a, "--ample")) {
+            o.por = 3; // single-process ample sets
+            i += 1;
+        } else if (!strcmp(a, "--stubborn")) {
+            o.por = 4; // stubborn sets from necessary enabling processes
             i += 1;
         } else if (!strcmp(a, "--cycle-proviso")) {
             if (o.property == GPX_PROP_NONE) o.cycle_proviso = 1; // only before -d/-p
@@ -179,7 +187,7 @@ int main(int argc, char **argv) {
             return 1;
         }
         fclose(pf);
-        if (o.por) o.por = 2;
+        if (o.por == 1) o.por = 2; // the proposal ranks cample's clusters
     }
     gpx_explorer *ex = nullptr;
     rc = gpx_explorer_create(m, &o, &ex);

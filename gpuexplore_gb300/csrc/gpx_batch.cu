@@ -50,6 +50,7 @@ struct __align__(128) BInst {
     unsigned long long *levels;
     unsigned long long max_states;
     uint32_t property, mode;
+    uint32_t por_kind, pad_kind;    // POR_CAMPLE / POR_AMPLE / POR_STUBBORN (job por 1-2 / 3 / 4)
     const gpx_por_model *por_model; // learned proposal (job por == 2), else null
 };
 
@@ -159,6 +160,7 @@ static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char 
     P.property = I->property;
     P.por_model = I->por_model;
     P.learned = I->por_model ? 1u : 0u;
+    P.por_kind = I->por_kind;
     Explorer<K128, MODE> E(P, I->model, *(WarpScratch<K128, MODE> *)raw);
     uint32_t B = kPairMax / E.M.n;
     B = B > 32 ? 32 : (B < 1 ? 1 : B);
@@ -429,6 +431,7 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
         if (prop_k == GPX_PROP_SAFETY && m->gpf.liveness == 1) prop_k = GPX_PROP_LIVENESS;
         h[k].property = (uint32_t)prop_k;
         h[k].mode = jobs[idx[k]].por ? (jobs[idx[k]].cycle_proviso ? MODE_PROVISO : MODE_POR) : MODE_PLAIN;
+        h[k].por_kind = jobs[idx[k]].por == 3 ? POR_AMPLE : (jobs[idx[k]].por == 4 ? POR_STUBBORN : POR_CAMPLE);
         h[k].ctrl.store_count = 1;
         h[k].ctrl.nlevels = 1;
         h[k].ctrl.hi = 1;
@@ -611,7 +614,8 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
     std::vector<uint64_t> cap(count, 0);
     for (uint32_t i = 0; i < count; i++) {
         memset(&items[i], 0, sizeof items[i]);
-        if (!models[i] || jobs[i].struct_size != sizeof(gpx_batch_job)) return GPX_ERR_INVALID;
+        if (!models[i] || jobs[i].struct_size != sizeof(gpx_batch_job) || jobs[i].por < 0 || jobs[i].por > 4)
+            return GPX_ERR_INVALID;
         // an instance too wide for 128-bit slots, or with a liveness property (the
         // accepting-cycle check runs through gpx_explorer_run only)
         if (models[i]->dec.state_bits > (uint32_t)kMaxStateBits ||

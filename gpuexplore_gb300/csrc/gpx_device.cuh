@@ -20,6 +20,9 @@ constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr int kPairMax = 256;   // (state, process) pairs staged per warp batch
 constexpr int kMaxProbe = 32;   // buckets probed before reporting the table full
 constexpr uint32_t kMaxLevels = 1u << 20;
+// cluster definitions of the POR modes: static clusters (cample), single-process
+// clusters only (ample), state-dependent necessary-enabling clusters (stubborn)
+enum PorKind : uint32_t { POR_CAMPLE = 0, POR_AMPLE = 1, POR_STUBBORN = 2 };
 constexpr unsigned long long kMaxLaunches = 2ull * kMaxLevels; // exploration launches per run
 
 enum Mode : int { MODE_PLAIN = 0, MODE_POR = 1, MODE_PROVISO = 2 };
@@ -72,6 +75,7 @@ struct Params {
     uint32_t property;
     uint32_t levels_per_launch;
     uint32_t total_warps;
+    uint32_t por_kind;      // POR_CAMPLE, POR_AMPLE or POR_STUBBORN
     // keys whose probe sequence was full, placed by the closing thread
     void *overflow;
     unsigned long long overflow_cap;
@@ -671,7 +675,7 @@ template <class K, int MODE> struct Explorer {
                         break;
                     }
                     psz *= grp[2];
-                    if (q == n - 1 && grp[3]) hit1 = true;
+                    if (q == n - 1 && (grp[3] & 1u)) hit1 = true;
                 }
                 if (ok) {
                     appl |= 1u << r;
@@ -683,7 +687,9 @@ template <class K, int MODE> struct Explorer {
             ws.appl[i] = appl;
             ws.pre[i] = cnt;
             if (MODE != MODE_PLAIN) {
-                ws.cl0[i] = rec[R_CL0];
+                // clusters feed the selection: the single POR pass, or the decide pass
+                if (MODE == MODE_POR || decide)
+                    ws.cl0[i] = P.por_kind == POR_STUBBORN ? stubborn_cluster(key, p, rec) : rec[R_CL0];
                 ws.nw[i] = 0;
             }
             if (lcnt | appl) ws.en[g] = 1;
@@ -797,6 +803,36 @@ template <class K, int MODE> struct Explorer {
     // leads); `prefix` when ws.pre already holds the exclusive prefix sum.
     __device__ uint32_t pair_succ(uint32_t i, bool prefix) const { return prefix ? ws.pre[i + 1] - ws.pre[i] : ws.pre[i]; }
 
+    // State-dependent cluster of process p (stubborn sets): {p}, and for every
+    // rule containing p of an action p has enabled, all its members if the rule
+    // is enabled, else only its lowest member without the action -- a necessary
+    // enabling process that must move before the rule can fire.  A subset of the
+    // static cluster (which takes every such rule whole).
+    __device__ uint32_t stubborn_cluster(const K &key, uint32_t p, const uint32_t *rec) const {
+        uint32_t cl = 1u << p;
+        const uint32_t nr = M.w[H_NRULES];
+        const uint32_t *g = M.sent_ + rec[R_SOFF] * 4;
+        for (uint32_t j = 0; j < rec[R_SCNT]; j++, g += 4) {
+            const uint32_t a = g[0];
+            for (uint32_t k = g[3] >> 1; k < nr && M.ract(k) == a; k++) {
+                const uint32_t mask = M.rmask(k);
+                if (!(mask >> p & 1u)) continue;
+                uint32_t lack = 0, rest = mask & ~(1u << p);
+                while (rest) {
+                    const uint32_t q = __ffs(rest) - 1;
+                    rest &= rest - 1;
+                    uint32_t sq;
+                    if (!M.group(M.state_rec(key, q, sq), a)) {
+                        lack = 1u << q;
+                        break;
+                    }
+                }
+                cl |= lack ? lack : mask;
+            }
+        }
+        return cl;
+    }
+
     // Features of candidate closure C of state g (GPX_POR_FEATURES small integers,
     // packed 4 per word): see include/gpx.h.
     __device__ void cluster_features(uint32_t g, uint32_t C, bool prefix, uint32_t (&xw)[10], uint32_t &succ) const {
@@ -856,7 +892,8 @@ template <class K, int MODE> struct Explorer {
                 closure |= cq;
             }
             ws.clo[i] = closure;
-            if (valid && closure) {
+            // ample: only a single process whose enabled transitions involve no other process
+            if (valid && closure && (P.por_kind != POR_AMPLE || __popc(closure) == 1)) {
                 atomicMin(&ws.best[g], ((uint32_t)__popc(closure) << 5) | p);
                 atomicOr(&ws.vmask[g], 1u << p);
             }

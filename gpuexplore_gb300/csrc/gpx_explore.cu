@@ -410,6 +410,9 @@ struct gpx_explorer {
 
 namespace {
 
+// gpx_options.por: 1 cample, 2 cample with the learned proposal, 3 ample, 4 stubborn
+uint32_t por_kind_of(int por) { return por == 3 ? POR_AMPLE : (por == 4 ? POR_STUBBORN : POR_CAMPLE); }
+
 int select_kind(uint32_t state_bits) {
     if (state_bits <= 31) return 0;
     if (state_bits <= 63) return 1;
@@ -492,6 +495,7 @@ Params make_params(gpx_explorer *ex) {
     P.levels_per_launch = ex->o.kernel_iters > 0 ? (uint32_t)ex->o.kernel_iters : 0;
     P.total_warps = (uint32_t)(ex->blocks * (ex->threads / 32));
     P.learned = (ex->o.por == 2 && ex->have_por_model) ? 1u : 0u;
+    P.por_kind = por_kind_of(ex->o.por);
     P.por_model = ex->have_por_model ? ex->d_por_model : nullptr;
     if (ex->d_log && ex->log_cap && ex->mode == MODE_PROVISO) {
         P.log = ex->d_log;
@@ -785,6 +789,7 @@ void gpx_explorer_destroy(gpx_explorer *ex) {
 int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_explorer **out) {
     if (!model || !opts || !out || opts->struct_size != sizeof(gpx_options)) return GPX_ERR_INVALID;
     if (opts->bucket_bytes != 0 && opts->bucket_bytes != 32) return GPX_ERR_INVALID;
+    if (opts->por < 0 || opts->por > 4) return GPX_ERR_INVALID;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPX_ERR_NO_GPU;
     if (opts->device < 0 || opts->device >= ndev) return GPX_ERR_INVALID;
@@ -1327,6 +1332,7 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     P.property = (uint32_t)property;
     P.levels_per_launch = opts->kernel_iters > 0 ? (uint32_t)opts->kernel_iters : 0;
     P.total_warps = (uint32_t)(blocks * (threads / 32));
+    P.por_kind = por_kind_of(opts->por);
 
     // clear what must start at zero (the array keeps the previous call's contents;
     // init_kernel resets the control block)

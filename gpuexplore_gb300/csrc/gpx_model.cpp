@@ -222,7 +222,7 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
                 sent.push_back(kv.first);
                 sent.push_back(toff);
                 sent.push_back((uint32_t)kv.second.size());
-                sent.push_back(has1);
+                sent.push_back(has1 | (rules_range[kv.first].first << 1)); // + first rule of the action
                 auto rr = rules_range[kv.first];
                 for (uint32_t k = rr.first; k < rr.first + rr.second; k++) {
                     uint32_t m = rule_mask[k];

@@ -65,7 +65,8 @@ enum RecIndex : int {
 };
 
 // Synchronising group (4 words): action, first target in stgt, target count,
-// bit 0 = some target is local state 1.
+// flags: bit 0 = some target is local state 1, bits 1.. = index of the action's
+// first rule (an action's rules are consecutive in the rules array).
 struct Decoded {
     uint32_t nprocs = 0;
     uint32_t state_bits = 0;

@@ -63,7 +63,8 @@ typedef struct {
     int32_t kernel_iters;   /* -k: BFS levels per kernel launch (0 = run to the end in one launch) */
     int32_t verbosity;      /* -v 0..3 (clamped to 3, GPUexplore.cu:1846-1848) */
     uint64_t q_words;       /* -q: hash-table size in 32-bit words (0 = half the free device memory) */
-    int32_t por;            /* --por: cluster-based ample-set reduction (2: with the learned proposal) */
+    int32_t por;            /* --por: 1 cluster-based ample sets (cample), 2 cample with the learned proposal,
+                               3 single-process ample sets, 4 stubborn sets (necessary-enabling clusters) */
     int32_t cycle_proviso;  /* --cycle-proviso */
     int32_t property;       /* gpx_property */
     int32_t device;         /* CUDA device ordinal */
@@ -280,7 +281,7 @@ int gpx_por_grad(int device, const float *w1, const float *b1, const float *w2, 
 typedef struct {
     uint32_t struct_size;
     int32_t property;       /* gpx_property */
-    int32_t por;            /* 0: none, 1: cluster POR, 2: cluster POR with the learned proposal */
+    int32_t por;            /* 0: none, 1: cluster POR, 2: cluster POR with the learned proposal, 3: ample, 4: stubborn */
     int32_t cycle_proviso;
     uint64_t max_states;    /* state budget (0 = none) */
     uint64_t capacity;      /* states admitted (table + store partition); 0 = estimate */

@@ -412,6 +412,31 @@ typedef struct {
     uint32_t s[MAXP];      /* local states */
 } por_ctx_t;
 
+/* Stubborn-set cluster of process p in state v: {p}, and for every rule
+ * containing p of an action p has enabled, the rule's members if every member
+ * has the action, else only its lowest member without it (a necessary enabling
+ * process).  A subset of static_cluster. */
+static uint32_t stubborn_cluster(const gpf_t *m, const expand_t *x, uint32_t p) {
+    uint32_t c = 1u << p, n = m->nr_procs, per = 32 / n;
+    for (uint32_t i = 0; i < x->nacts[p]; i++) {
+        uint32_t a = x->acts[p][i].act, r1, r2;
+        rule_range(m, a, &r1, &r2);
+        for (uint32_t w = r1; w < r2 && w < m->nr_syncbits; w++)
+            for (uint32_t f = 0; f < per; f++) {
+                uint32_t rule = (m->syncbits[w] >> (f * n)) & ((1u << n) - 1u);
+                if (!(rule >> p & 1u)) continue;
+                uint32_t lack = 0;
+                for (uint32_t q = 0; q < n && !lack; q++)
+                    if ((rule >> q & 1u) && !find_act(x, q, a)) lack = 1u << q;
+                c |= lack ? lack : rule;
+            }
+    }
+    return c;
+}
+
+/* ample: only single-process closures qualify */
+static int g_ample = 0;
+
 static uint32_t select_cluster(uint32_t n, const uint32_t *cl, uint32_t prov, const por_ctx_t *pc) {
     uint32_t c[MAXP];
     for (uint32_t p = 0; p < n; p++) c[p] = (prov >> p & 1u) ? cl[p] : (cl[p] & ~(1u << p));
@@ -428,7 +453,8 @@ static uint32_t select_cluster(uint32_t n, const uint32_t *cl, uint32_t prov, co
             todo |= c[i] & ~closure & ~(1u << i);
             closure |= c[i];
         }
-        if (valid && closure && (uint32_t)__builtin_popcount(closure) < bestc) {
+        if (valid && closure && (!g_ample || __builtin_popcount(closure) == 1) &&
+            (uint32_t)__builtin_popcount(closure) < bestc) {
             bestc = (uint32_t)__builtin_popcount(closure);
             best = closure;
         }
@@ -658,7 +684,7 @@ static uint32_t decide(sctx_t *c, const uint32_t *v, expand_t *x, int *deadlock)
     if (!c->o->por) return 0xFFFFFFFFu;
     uint32_t cl[MAXP];
     for (uint32_t p = 0; p < m->nr_procs; p++) {
-        cl[p] = static_cluster(m, x, p);
+        cl[p] = c->o->por == 4 ? stubborn_cluster(m, x, p) : static_cluster(m, x, p);
         c->pc.nlocal[p] = x->nlocal[p];
         c->pc.s[p] = get_local(m, v, p);
     }
@@ -957,7 +983,7 @@ static int liveness_check(const gpf_t *m, hset_t *shards, uint32_t S, uint64_t *
 
 static void usage(void) {
     fprintf(stderr,
-            "usage: gpx_oracle <model>[.gpf] [-d|-p] [--por] [--cycle-proviso] [--threads N]\n"
+            "usage: gpx_oracle <model>[.gpf] [-d|-p] [--por|--ample|--stubborn] [--cycle-proviso] [--threads N]\n"
             "                  [--max-states N] [--dump-states FILE]\n");
 }
 
@@ -993,6 +1019,11 @@ int main(int argc, char **argv) {
             o.por = 2;
         } else if (!strcmp(argv[i], "--por")) {
             if (!o.por) o.por = 1;
+        } else if (!strcmp(argv[i], "--ample")) {
+            o.por = 3;
+            g_ample = 1;
+        } else if (!strcmp(argv[i], "--stubborn")) {
+            o.por = 4;
         } else if (!strcmp(argv[i], "--cycle-proviso")) {
             if (o.property == PROP_NONE) o.proviso = 1;
         } else if (!strcmp(argv[i], "--threads") && i + 1 < argc) {

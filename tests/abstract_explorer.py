@@ -58,7 +58,25 @@ def static_clusters(net: Network, s: State) -> List[int]:
     return cl
 
 
-def select_cluster(n: int, cl: List[int], prov: int) -> int:
+def stubborn_clusters(net: Network, s: State) -> List[int]:
+    """Per process: itself, and for each rule containing it of an action it has
+    enabled, the rule's members if all have the action, else the rule's lowest
+    member without it (a necessary enabling process)."""
+    n = net.nprocs
+    cl = []
+    for p in range(n):
+        c = 1 << p
+        for a in net.sync[p][s[p]]:
+            for r in net.rules.get(a, []):
+                if not r >> p & 1:
+                    continue
+                lack = [q for q in range(n) if r >> q & 1 and a not in net.sync[q][s[q]]]
+                c |= (1 << lack[0]) if lack else r
+        cl.append(c)
+    return cl
+
+
+def select_cluster(n: int, cl: List[int], prov: int, ample: bool = False) -> int:
     c = [cl[p] if prov >> p & 1 else cl[p] & ~(1 << p) for p in range(n)]
     best, bestc = (1 << n) - 1, n
     for p in range(n):
@@ -73,13 +91,16 @@ def select_cluster(n: int, cl: List[int], prov: int) -> int:
                     seen.add(j)
                     stack.append(j)
         valid = any(c[i] >> i & 1 for i in range(n) if closure >> i & 1)
-        if valid and closure and bin(closure).count("1") < bestc:
+        if valid and closure and (not ample or bin(closure).count("1") == 1) and bin(closure).count("1") < bestc:
             bestc, best = bin(closure).count("1"), closure
     return best
 
 
 def explore(net: Network, prop: str = "none", por: bool = False, proviso: bool = False,
-            max_states: int = 0) -> Dict:
+            max_states: int = 0, kind: str = "cample") -> Dict:
+    """BFS; with `por`, the cluster reduction of `kind`: "cample" (static
+    clusters), "ample" (single-process clusters only) or "stubborn"
+    (necessary-enabling clusters)."""
     n = net.nprocs
     init: State = tuple([0] * n)
     visited: Set[State] = {init}
@@ -103,7 +124,8 @@ def explore(net: Network, prop: str = "none", por: bool = False, proviso: bool =
                 for t, mask in succ:
                     if not proviso or t not in visited:
                         prov |= mask
-                sel = select_cluster(n, static_clusters(net, s), prov)
+                cl = stubborn_clusters(net, s) if kind == "stubborn" else static_clusters(net, s)
+                sel = select_cluster(n, cl, prov, ample=kind == "ample")
             decisions[s] = sel
         for s in frontier:
             sel = decisions[s]

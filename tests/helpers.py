@@ -14,6 +14,11 @@ FLAGS = {
     "por_proviso": (["--por", "--cycle-proviso"], {"por": 1, "cycle_proviso": 1}),
     "por_safety": (["--por", "-p"], {"por": 1, "cycle_proviso": 1, "property": "safety"}),
     "por_deadlock": (["--por", "-d"], {"por": 1, "property": "deadlock"}),
+    "ample_deadlock": (["--ample", "-d"], {"por": 3, "property": "deadlock"}),
+    "ample_safety": (["--ample", "-p"], {"por": 3, "cycle_proviso": 1, "property": "safety"}),
+    "stubborn_proviso": (["--stubborn", "--cycle-proviso"], {"por": 4, "cycle_proviso": 1}),
+    "stubborn_deadlock": (["--stubborn", "-d"], {"por": 4, "property": "deadlock"}),
+    "stubborn_safety": (["--stubborn", "-p"], {"por": 4, "cycle_proviso": 1, "property": "safety"}),
 }
 
 

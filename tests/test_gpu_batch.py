@@ -9,7 +9,8 @@ from helpers import FLAGS, oracle, write_net
 
 pytestmark = pytest.mark.gpu
 
-FLAGSET = ["plain", "deadlock", "safety", "por", "por_proviso", "por_safety"]
+FLAGSET = ["plain", "deadlock", "safety", "por", "por_proviso", "por_safety", "ample_safety", "stubborn_deadlock",
+           "stubborn_safety"]
 
 
 def _batch_cases(n, seed):
@@ -40,9 +41,10 @@ def _check(lib, tmp_path, cases, **opts):
         want.append(oracle(path, cli, max_states=job["max_states"]))
         models.append(lib.Model.from_file(path))
         jobs.append(job)
-    items, stats = lib.batch_explore(models, jobs, **opts)
+    items, stats = lib.batch_explore(models, jobs, level_capacity=4096, **opts)
     for k, (it, w) in enumerate(zip(items, want)):
         assert it["status"] == 0, (k, it)
+        assert it["nlevels"] == len(w["levels"]), k
         for key in ("states", "levels", "verdict", "stopped", "set_hash"):
             assert it[key] == w[key], (k, cases[k][1], key, it[key], w[key])
     assert stats["states"] == sum(w["states"] for w in want)

@@ -23,7 +23,8 @@ def _count(stdout):
 
 
 @pytest.mark.parametrize("flags,expect", [([], None), (["-d"], "deadlock"), (["-p"], "safety"),
-                                          (["--por", "--cycle-proviso"], None)])
+                                          (["--por", "--cycle-proviso"], None),
+                                          (["--stubborn", "-d"], "deadlock"), (["--ample", "-p"], "safety")])
 def test_cli_matches_oracle(gpu, built, tmp_path, flags, expect):
     net = gen.random_network(16, nprocs=9, states=(3, 6), outdeg=(1, 2), sync_frac=0.7) if expect == "deadlock" \
         else gen.ring(2)
