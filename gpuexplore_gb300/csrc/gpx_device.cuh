@@ -18,6 +18,7 @@ namespace gpx {
 
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr int kPairMax = 256;   // (state, process) pairs staged per warp batch
+constexpr int kPairMaxPor = 160; // ... with POR: its per-pair arrays then fit 4 blocks per SM
 constexpr int kMaxProbe = 32;   // buckets probed before reporting the table full
 constexpr uint32_t kMaxLevels = 1u << 20;
 // cluster definitions of the POR modes: static clusters (cample), single-process
@@ -392,11 +393,12 @@ __device__ __forceinline__ bool find_key(K *table, unsigned long long nb, const 
 constexpr int kStage = 64; // new states staged per warp before one store append
 
 template <class K, int MODE> struct WarpScratch {
-    static constexpr int kPor = (MODE == MODE_PLAIN) ? 1 : kPairMax;
+    static constexpr int kPairs = (MODE == MODE_PLAIN) ? kPairMax : kPairMaxPor;
+    static constexpr int kPor = (MODE == MODE_PLAIN) ? 1 : kPairs;
     K keys[32];                  // the batch's source states
     K stage[kStage];             // new states waiting to be appended to the store
-    uint32_t appl[kPairMax];     // per pair: applicable rules among those it leads (bit r)
-    uint32_t pre[kPairMax + 1];  // per pair: successor count, then its exclusive prefix sum
+    uint32_t appl[kPairs];       // per pair: applicable rules among those it leads (bit r)
+    uint32_t pre[kPairs + 1];    // per pair: successor count, then its exclusive prefix sum
     uint32_t en[32];             // per state: some transition enabled
     uint32_t cl0[kPor];          // per pair: static POR cluster
     uint32_t clo[kPor];          // per pair: cluster closure

@@ -162,7 +162,7 @@ template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_k
 
     Explorer<K, MODE> E(P, model, ws);
     const uint32_t n = E.M.n;
-    uint32_t Bmax = kPairMax / n;
+    uint32_t Bmax = WarpScratch<K, MODE>::kPairs / n;
     if (Bmax > 32) Bmax = 32;
     if (Bmax < 1) Bmax = 1;
     // every warp's first claim of a phase is static (warp gw takes
