@@ -174,19 +174,29 @@ template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_k
         const uint32_t B = claim < Bmax ? claim : Bmax;
         const bool decide = (MODE == MODE_PROVISO) && view.phase == PH_DECIDE;
         const unsigned long long static_end = (unsigned long long)P.total_warps * claim;
-        unsigned long long base = gw * claim;
+        unsigned long long base = gw * claim, size = claim;
         while (base < nlev) {
-            unsigned long long end = base + claim < nlev ? base + claim : nlev;
+            unsigned long long end = base + size < nlev ? base + size : nlev;
             for (unsigned long long b = base; b < end; b += B) {
                 uint32_t cnt = (uint32_t)((end - b) < B ? (end - b) : B);
                 E.batch(lo + b, cnt, b, decide);
             }
             if (static_end >= nlev) break;
             base = nlev;
-            // read before contending: late in a level most warps find nothing to claim
-            if (E.lane == 0 && static_end + vload(&c->cursor) < nlev && !vload(&c->error))
-                base = static_end + atomicAdd(&c->cursor, (unsigned long long)claim);
+            // guided self-scheduling: a quarter of a fair share of what is left
+            // (between one full batch and `claim`), so the level drains in ever
+            // smaller claims instead of ending on a few warps busy with full-size
+            // ones; read before contending
+            if (E.lane == 0) {
+                const unsigned long long cur = vload(&c->cursor);
+                if (static_end + cur < nlev && !vload(&c->error)) {
+                    unsigned long long g = (nlev - static_end - cur) / (4ull * P.total_warps);
+                    size = g < B ? B : (g > claim ? claim : g);
+                    base = static_end + atomicAdd(&c->cursor, size);
+                }
+            }
             base = __shfl_sync(kFull, base, 0);
+            size = __shfl_sync(kFull, size, 0);
         }
         E.flush_level();
         grid_barrier<K, MODE>(P, view);
