@@ -226,7 +226,8 @@ def run_other_workload(args, local):
                 live.append(r["live_ms"])
             ex.close()
             per[name] = {"states": r["states"], "verdict": r["verdict"], "explore_ms": statistics.median(ker),
-                         "check_ms": statistics.median(live), "fixpoint_states": r["live_states"]}
+                         "check_ms": statistics.median(live), "fixpoint_states": r["live_states"],
+                         "check_rounds": r["live_rounds"]}
         h = per["holds"]
         value = h["states"] / ((h["explore_ms"] + h["check_ms"]) / 1000.0)
         line.update(metric="states checked/s (exploration + accepting-cycle check)", value=value,

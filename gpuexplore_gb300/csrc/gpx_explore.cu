@@ -1008,8 +1008,8 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
         // the whole state space is in the table: look for an accepting cycle
         unsigned long long left = 0, rounds = 0;
         GPX_CUDA(cudaEventRecord(ex->ev[0], ex->st));
-        int rc = live_check(ex->kind, ex->d_table, ex->nbuckets, ex->slots, count, ex->d_model, ex->o.seed, ex->st,
-                            &ex->live, &left, &rounds);
+        int rc = live_check(ex->kind, ex->d_table, ex->nbuckets, ex->slots, ex->d_store, count, ex->d_model,
+                            ex->o.seed, ex->st, &ex->live, &left, &rounds);
         if (rc != GPX_OK) return rc;
         GPX_CUDA(cudaEventRecord(ex->ev[1], ex->st));
         GPX_CUDA(cudaEventSynchronize(ex->ev[1]));
@@ -1017,6 +1017,7 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
         cudaEventElapsedTime(&ms, ex->ev[0], ex->ev[1]);
         r->live_ms = ms;
         r->live_states = left;
+        r->live_rounds = rounds;
         if (left) {
             r->verdict = GPX_PROP_LIVENESS;
             r->stopped = GPX_STOP_VIOLATION;

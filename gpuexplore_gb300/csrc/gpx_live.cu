@@ -4,8 +4,10 @@
 // never checked.  Here it means: the last process is a Buchi automaton whose
 // local state 1 is accepting, and the property is violated iff a reachable
 // cycle passes through an accepting state.  The check runs after a complete
-// exploration (no POR) on the hash table itself, a state's identity being its
-// slot, with the One-Way-Catch-Them-Young fixpoint (Cerna and Pelanek, 2003):
+// exploration (no POR) over the state store (a state's identity is its store
+// position, found from a successor through its table slot and a slot -> position
+// map written once), with the One-Way-Catch-Them-Young fixpoint (Cerna and
+// Pelanek, 2003):
 //
 //   S := visited states
 //   repeat
@@ -98,59 +100,73 @@ template <class K, class F> __device__ void for_each_successor(const MView &M, c
     }
 }
 
-__device__ __forceinline__ void push(unsigned long long *front, unsigned long long *n, unsigned long long cap,
-                                     unsigned long long slot, unsigned long long *overflow) {
+__device__ __forceinline__ void push(uint32_t *front, unsigned long long *n, unsigned long long cap, uint32_t i,
+                                     unsigned long long *overflow) {
     const unsigned long long k = atomicAdd(n, 1ull);
     if (k < cap)
-        front[k] = slot;
+        front[k] = i;
     else
         atomicAdd(overflow, 1ull);
 }
 
-// count[0]: |S|, count[1]: frontier size, count[2]: next frontier size, count[3]: overflow / missing slots
-template <class K> __global__ void live_init_kernel(const K *table, unsigned long long slots, uint32_t *flag,
-                                                    uint32_t *indeg, unsigned long long *count) {
-    unsigned long long acc = 0;
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+// Store position of a successor (~0u when it is missing from the table).
+template <class K>
+__device__ __forceinline__ uint32_t position_of(const K *table, unsigned long long nb, const uint32_t *index,
+                                                const K &v, unsigned long long seed) {
+    const unsigned long long j = find_slot(table, nb, v, KT<K>::hash(v, seed));
+    return j == ~0ull ? ~0u : __ldg(index + j);
+}
+
+// count[0]: |S|, count[1]: frontier size, count[2]: next frontier size, count[3]: overflow / missing states
+
+// The slot -> store position map, and S := every state.
+template <class K>
+__global__ void live_init_kernel(const K *table, unsigned long long nb, const K *store, unsigned long long states,
+                                 unsigned long long seed, uint32_t *index, uint32_t *flag, uint32_t *indeg,
+                                 unsigned long long *count) {
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < states;
          i += (unsigned long long)gridDim.x * blockDim.x) {
-        const bool occ = !KT<K>::empty(KT<K>::load(table + i));
-        flag[i] = occ ? kInSet : 0u;
+        const K key = KT<K>::load(store + i);
+        const unsigned long long j = find_slot(table, nb, key, KT<K>::hash(key, seed));
+        if (j == ~0ull)
+            atomicAdd(&count[3], 1ull);
+        else
+            index[j] = (uint32_t)i;
+        flag[i] = kInSet;
         indeg[i] = 0;
-        acc += occ;
     }
-    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
-    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&count[0], acc);
 }
 
 // Mark the accepting states of S and put them in the frontier.
 template <class K>
-__global__ void live_seed_kernel(const K *table, unsigned long long slots, const uint32_t *model, uint32_t *flag,
-                                 unsigned long long *front, unsigned long long cap, unsigned long long *count) {
+__global__ void live_seed_kernel(const K *store, unsigned long long states, const uint32_t *model, uint32_t *flag,
+                                 uint32_t *front, unsigned long long cap, unsigned long long *count) {
     MView M;
     M.init(model);
     const uint32_t d = M.pd(M.n - 1);
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < states;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         if (!(flag[i] & kInSet)) continue;
-        if (KT<K>::get(KT<K>::load(table + i), MView::fb_of(d), MView::bs_of(d)) != 1) continue;
+        if (KT<K>::get(KT<K>::load(store + i), MView::fb_of(d), MView::bs_of(d)) != 1) continue;
         flag[i] |= kMarked;
-        push(front, &count[1], cap, i, &count[3]);
+        push(front, &count[1], cap, (uint32_t)i, &count[3]);
     }
 }
 
 // One forward round: mark the unmarked successors in S of the frontier.
 template <class K>
-__global__ void live_reach_kernel(const K *table, unsigned long long nb, const uint32_t *model, unsigned long long seed,
-                                  uint32_t *flag, const unsigned long long *front, unsigned long long nfront,
-                                  unsigned long long *next, unsigned long long cap, unsigned long long *count) {
+__global__ void live_reach_kernel(const K *table, unsigned long long nb, const uint32_t *index, const K *store,
+                                  const uint32_t *model, unsigned long long seed, uint32_t *flag, const uint32_t *front,
+                                  unsigned long long nfront, uint32_t *next, unsigned long long cap,
+                                  unsigned long long *count) {
     MView M;
     M.init(model);
     for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; t < nfront;
          t += (unsigned long long)gridDim.x * blockDim.x) {
-        const K key = KT<K>::load(table + front[t]);
+        const K key = KT<K>::load(store + front[t]);
         for_each_successor(M, key, [&](const K &v) {
-            const unsigned long long j = find_slot(table, nb, v, KT<K>::hash(v, seed));
-            if (j == ~0ull) {
+            const uint32_t j = position_of(table, nb, index, v, seed);
+            if (j == ~0u) {
                 atomicAdd(&count[3], 1ull);
                 return;
             }
@@ -159,11 +175,11 @@ __global__ void live_reach_kernel(const K *table, unsigned long long nb, const u
     }
 }
 
-// S := marked states of S; clears the marks; counts |S|.
-__global__ void live_restrict_kernel(unsigned long long slots, uint32_t *flag, uint32_t *indeg,
+// S := marked states of S; clears the marks and the predecessor counts; counts |S|.
+__global__ void live_restrict_kernel(unsigned long long states, uint32_t *flag, uint32_t *indeg,
                                      unsigned long long *count) {
     unsigned long long acc = 0;
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < states;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         const uint32_t f = flag[i];
         const uint32_t keep = (f & kInSet) && (f & kMarked) ? kInSet : 0u;
@@ -177,18 +193,18 @@ __global__ void live_restrict_kernel(unsigned long long slots, uint32_t *flag, u
 
 // Predecessor counts inside S (edges counted with multiplicity).
 template <class K>
-__global__ void live_indeg_kernel(const K *table, unsigned long long nb, unsigned long long slots,
-                                  const uint32_t *model, unsigned long long seed, const uint32_t *flag,
-                                  uint32_t *indeg, unsigned long long *count) {
+__global__ void live_indeg_kernel(const K *table, unsigned long long nb, const uint32_t *index, const K *store,
+                                  unsigned long long states, const uint32_t *model, unsigned long long seed,
+                                  const uint32_t *flag, uint32_t *indeg, unsigned long long *count) {
     MView M;
     M.init(model);
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < states;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         if (!(flag[i] & kInSet)) continue;
-        const K key = KT<K>::load(table + i);
+        const K key = KT<K>::load(store + i);
         for_each_successor(M, key, [&](const K &v) {
-            const unsigned long long j = find_slot(table, nb, v, KT<K>::hash(v, seed));
-            if (j == ~0ull) {
+            const uint32_t j = position_of(table, nb, index, v, seed);
+            if (j == ~0u) {
                 atomicAdd(&count[3], 1ull);
                 return;
             }
@@ -198,30 +214,30 @@ __global__ void live_indeg_kernel(const K *table, unsigned long long nb, unsigne
 }
 
 // The states of S without predecessors in S start the peeling.
-__global__ void live_sources_kernel(unsigned long long slots, const uint32_t *flag, const uint32_t *indeg,
-                                    unsigned long long *front, unsigned long long cap, unsigned long long *count) {
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+__global__ void live_sources_kernel(unsigned long long states, const uint32_t *flag, const uint32_t *indeg,
+                                    uint32_t *front, unsigned long long cap, unsigned long long *count) {
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < states;
          i += (unsigned long long)gridDim.x * blockDim.x)
-        if ((flag[i] & kInSet) && indeg[i] == 0) push(front, &count[1], cap, i, &count[3]);
+        if ((flag[i] & kInSet) && indeg[i] == 0) push(front, &count[1], cap, (uint32_t)i, &count[3]);
 }
 
 // One peeling round: remove the frontier from S; successors whose last
 // predecessor in S went form the next frontier.
 template <class K>
-__global__ void live_peel_kernel(const K *table, unsigned long long nb, const uint32_t *model, unsigned long long seed,
-                                 uint32_t *flag, uint32_t *indeg, const unsigned long long *front,
-                                 unsigned long long nfront, unsigned long long *next, unsigned long long cap,
-                                 unsigned long long *count) {
+__global__ void live_peel_kernel(const K *table, unsigned long long nb, const uint32_t *index, const K *store,
+                                 const uint32_t *model, unsigned long long seed, uint32_t *flag, uint32_t *indeg,
+                                 const uint32_t *front, unsigned long long nfront, uint32_t *next,
+                                 unsigned long long cap, unsigned long long *count) {
     MView M;
     M.init(model);
     for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; t < nfront;
          t += (unsigned long long)gridDim.x * blockDim.x) {
-        const unsigned long long i = front[t];
+        const uint32_t i = front[t];
         flag[i] = 0;
-        const K key = KT<K>::load(table + i);
+        const K key = KT<K>::load(store + i);
         for_each_successor(M, key, [&](const K &v) {
-            const unsigned long long j = find_slot(table, nb, v, KT<K>::hash(v, seed));
-            if (j == ~0ull) {
+            const uint32_t j = position_of(table, nb, index, v, seed);
+            if (j == ~0u) {
                 atomicAdd(&count[3], 1ull);
                 return;
             }
@@ -230,9 +246,9 @@ __global__ void live_peel_kernel(const K *table, unsigned long long nb, const ui
     }
 }
 
-__global__ void live_count_kernel(unsigned long long slots, const uint32_t *flag, unsigned long long *count) {
+__global__ void live_count_kernel(unsigned long long states, const uint32_t *flag, unsigned long long *count) {
     unsigned long long acc = 0;
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < states;
          i += (unsigned long long)gridDim.x * blockDim.x)
         acc += flag[i] & kInSet;
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
@@ -240,6 +256,7 @@ __global__ void live_count_kernel(unsigned long long slots, const uint32_t *flag
 }
 
 void live_free(LiveScratch *s) {
+    cudaFree(s->index);
     cudaFree(s->flag);
     cudaFree(s->indeg);
     cudaFree(s->front[0]);
@@ -265,25 +282,23 @@ int grid_for(unsigned long long n) {
 }
 
 template <class K>
-int run(const K *table, unsigned long long nb, unsigned long long slots, unsigned long long states,
+int run(const K *table, unsigned long long nb, unsigned long long slots, const K *store, unsigned long long states,
         const uint32_t *model, unsigned long long seed, cudaStream_t st, LiveScratch *s,
         unsigned long long *set_states, unsigned long long *rounds) {
+    if (states >= 0xFFFFFFFFull) return GPX_ERR_UNSUPPORTED; // store positions are 32-bit
     if (s->slots < slots) {
-        cudaFree(s->flag);
-        cudaFree(s->indeg);
-        s->flag = nullptr;
-        s->indeg = nullptr;
-        LCUDA(cudaMalloc(&s->flag, slots * 4));
-        LCUDA(cudaMalloc(&s->indeg, slots * 4));
+        cudaFree(s->index);
+        s->index = nullptr;
+        LCUDA(cudaMalloc(&s->index, slots * 4));
         s->slots = slots;
     }
-    if (s->front_cap < states) {
-        for (auto &f : s->front) {
-            cudaFree(f);
-            f = nullptr;
-            LCUDA(cudaMalloc(&f, states * 8));
+    if (s->states < states) {
+        for (uint32_t **a : {&s->flag, &s->indeg, &s->front[0], &s->front[1]}) {
+            cudaFree(*a);
+            *a = nullptr;
+            LCUDA(cudaMalloc(a, states * 4));
         }
-        s->front_cap = states;
+        s->states = states;
     }
     if (!s->count) LCUDA(cudaMalloc(&s->count, 4 * 8));
     unsigned long long h[4];
@@ -296,27 +311,29 @@ int run(const K *table, unsigned long long nb, unsigned long long slots, unsigne
         }
         return GPX_OK;
     };
-    const int gs = grid_for(slots);
+    const unsigned long long cap = s->states;
+    const int gs = grid_for(states);
     *rounds = 0;
     LCUDA(cudaMemsetAsync(s->count, 0, sizeof h, st));
-    live_init_kernel<K><<<gs, 256, 0, st>>>(table, slots, s->flag, s->indeg, s->count);
+    live_init_kernel<K><<<gs, 256, 0, st>>>(table, nb, store, states, seed, s->index, s->flag, s->indeg, s->count);
     LCUDA(cudaGetLastError());
     int rc = read();
     if (rc) return rc;
-    unsigned long long size = h[0];
+    unsigned long long size = states;
     for (;;) {
         const unsigned long long before = size;
         // forward closure from the accepting states of S
         LCUDA(cudaMemsetAsync(s->count, 0, sizeof h, st));
-        live_seed_kernel<K><<<gs, 256, 0, st>>>(table, slots, model, s->flag, s->front[0], s->front_cap, s->count);
+        live_seed_kernel<K><<<gs, 256, 0, st>>>(store, states, model, s->flag, s->front[0], cap, s->count);
         LCUDA(cudaGetLastError());
         if ((rc = read())) return rc;
         int cur = 0;
         unsigned long long nfront = h[1];
         while (nfront) {
             LCUDA(cudaMemsetAsync(s->count + 2, 0, 8, st));
-            live_reach_kernel<K><<<grid_for(nfront), 256, 0, st>>>(table, nb, model, seed, s->flag, s->front[cur],
-                                                                   nfront, s->front[cur ^ 1], s->front_cap, s->count);
+            live_reach_kernel<K><<<grid_for(nfront), 256, 0, st>>>(table, nb, s->index, store, model, seed, s->flag,
+                                                                   s->front[cur], nfront, s->front[cur ^ 1], cap,
+                                                                   s->count);
             LCUDA(cudaGetLastError());
             if ((rc = read())) return rc;
             nfront = h[2];
@@ -324,25 +341,26 @@ int run(const K *table, unsigned long long nb, unsigned long long slots, unsigne
             ++*rounds;
         }
         LCUDA(cudaMemsetAsync(s->count, 0, sizeof h, st));
-        live_restrict_kernel<<<gs, 256, 0, st>>>(slots, s->flag, s->indeg, s->count);
+        live_restrict_kernel<<<gs, 256, 0, st>>>(states, s->flag, s->indeg, s->count);
         LCUDA(cudaGetLastError());
         if ((rc = read())) return rc;
         size = h[0];
         if (size == 0) break;
         // peel the states with no predecessor in S
         LCUDA(cudaMemsetAsync(s->count, 0, sizeof h, st));
-        live_indeg_kernel<K><<<gs, 256, 0, st>>>(table, nb, slots, model, seed, s->flag, s->indeg, s->count);
+        live_indeg_kernel<K><<<gs, 256, 0, st>>>(table, nb, s->index, store, states, model, seed, s->flag, s->indeg,
+                                                 s->count);
         LCUDA(cudaGetLastError());
-        live_sources_kernel<<<gs, 256, 0, st>>>(slots, s->flag, s->indeg, s->front[0], s->front_cap, s->count);
+        live_sources_kernel<<<gs, 256, 0, st>>>(states, s->flag, s->indeg, s->front[0], cap, s->count);
         LCUDA(cudaGetLastError());
         if ((rc = read())) return rc;
         cur = 0;
         nfront = h[1];
         while (nfront) {
             LCUDA(cudaMemsetAsync(s->count + 2, 0, 8, st));
-            live_peel_kernel<K><<<grid_for(nfront), 256, 0, st>>>(table, nb, model, seed, s->flag, s->indeg,
-                                                                  s->front[cur], nfront, s->front[cur ^ 1],
-                                                                  s->front_cap, s->count);
+            live_peel_kernel<K><<<grid_for(nfront), 256, 0, st>>>(table, nb, s->index, store, model, seed, s->flag,
+                                                                  s->indeg, s->front[cur], nfront, s->front[cur ^ 1],
+                                                                  cap, s->count);
             LCUDA(cudaGetLastError());
             if ((rc = read())) return rc;
             nfront = h[2];
@@ -350,7 +368,7 @@ int run(const K *table, unsigned long long nb, unsigned long long slots, unsigne
             ++*rounds;
         }
         LCUDA(cudaMemsetAsync(s->count, 0, sizeof h, st));
-        live_count_kernel<<<gs, 256, 0, st>>>(slots, s->flag, s->count);
+        live_count_kernel<<<gs, 256, 0, st>>>(states, s->flag, s->count);
         LCUDA(cudaGetLastError());
         if ((rc = read())) return rc;
         size = h[0];
@@ -362,14 +380,17 @@ int run(const K *table, unsigned long long nb, unsigned long long slots, unsigne
 
 } // namespace
 
-int live_check(int kind, void *table, unsigned long long nbuckets, unsigned long long slots,
+int live_check(int kind, void *table, unsigned long long nbuckets, unsigned long long slots, const void *store,
                unsigned long long states, const uint32_t *model, unsigned long long seed, cudaStream_t st,
                LiveScratch *s, unsigned long long *set_states, unsigned long long *rounds) {
     if (kind == 0)
-        return run<K32>((const K32 *)table, nbuckets, slots, states, model, seed, st, s, set_states, rounds);
+        return run<K32>((const K32 *)table, nbuckets, slots, (const K32 *)store, states, model, seed, st, s,
+                        set_states, rounds);
     if (kind == 1)
-        return run<K64>((const K64 *)table, nbuckets, slots, states, model, seed, st, s, set_states, rounds);
-    return run<K128>((const K128 *)table, nbuckets, slots, states, model, seed, st, s, set_states, rounds);
+        return run<K64>((const K64 *)table, nbuckets, slots, (const K64 *)store, states, model, seed, st, s,
+                        set_states, rounds);
+    return run<K128>((const K128 *)table, nbuckets, slots, (const K128 *)store, states, model, seed, st, s,
+                     set_states, rounds);
 }
 
 } // namespace gpx

@@ -87,6 +87,7 @@ class Result(C.Structure):
         ("table_slots", C.c_uint64), ("slot_bytes", C.c_uint32), ("blocks", C.c_uint32), ("threads", C.c_uint32),
         ("inserts", C.c_uint64), ("evictions", C.c_uint64),
         ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("live_states", C.c_uint64), ("live_ms", C.c_double),
+        ("live_rounds", C.c_uint64),
     ]
 
 
@@ -266,7 +267,7 @@ def _result_dict(r: Result) -> Dict:
         "transitions": int(r.transitions), "probes": int(r.probes), "lookups": int(r.lookups),
         "inserts": int(r.inserts), "evictions": int(r.evictions),
         "h2d_bytes": int(r.h2d_bytes), "d2h_bytes": int(r.d2h_bytes), "live_states": int(r.live_states),
-        "live_ms": float(r.live_ms),
+        "live_ms": float(r.live_ms), "live_rounds": int(r.live_rounds),
         "expanded": int(r.expanded), "launches": int(r.launches), "explore_ms": float(r.explore_ms),
         "kernel_ms": float(r.kernel_ms), "setup_ms": float(r.setup_ms), "set_hash": f"{r.set_hash:016x}",
         "key_words": int(r.key_words), "table_count": int(r.table_count), "table_slots": int(r.table_slots),

@@ -109,6 +109,7 @@ typedef struct {
     uint64_t d2h_bytes;      /* bytes this run copied device -> host (without collect_states / -v output) */
     uint64_t live_states;    /* liveness: states left in the accepting-cycle fixpoint (0 = no accepting cycle) */
     double live_ms;          /* liveness: device time of the accepting-cycle check */
+    uint64_t live_rounds;    /* liveness: frontier rounds (forward closure and peeling) of the check */
 } gpx_result;
 
 typedef struct gpx_model gpx_model;
