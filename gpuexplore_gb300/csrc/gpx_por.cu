@@ -109,17 +109,23 @@ __global__ void grad_w1_kernel(const uint8_t *x, uint32_t rows, const float *dpr
         for (int j = 0; j < F; j++) acc[j] = fmaf(d, (float)x[(size_t)r * F + j] * kInScale, acc[j]);
         acc[F] += d;
     }
-    __shared__ float red[F + 1];
-    if (threadIdx.x <= F) red[threadIdx.x] = 0;
-    __syncthreads();
+    // per-warp partial sums, then one fixed-order sum over the warps: the
+    // gradient (and so training) does not depend on warp scheduling
+    __shared__ float part[8][F + 1];
     for (int j = 0; j <= F; j++) {
         float v = acc[j];
         for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
-        if ((threadIdx.x & 31) == 0) atomicAdd(&red[j], v);
+        if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5][j] = v;
     }
     __syncthreads();
-    if (threadIdx.x < F) g[k * F + threadIdx.x] = red[threadIdx.x];
-    if (threadIdx.x == F) g[H * F + k] = red[F];
+    if (threadIdx.x <= F) {
+        float v = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += part[w][threadIdx.x];
+        if (threadIdx.x < F)
+            g[k * F + threadIdx.x] = v;
+        else
+            g[H * F + k] = v;
+    }
 }
 
 __global__ void grad_w2_kernel(uint32_t rows, const float *hid, const float *dout, float *g) {
@@ -127,12 +133,14 @@ __global__ void grad_w2_kernel(uint32_t rows, const float *hid, const float *dou
     float acc = 0;
     for (uint32_t r = threadIdx.x; r < rows; r += blockDim.x) acc += (k < H ? hid[(size_t)r * H + k] : 1.0f) * dout[r];
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
-    __shared__ float red;
-    if (threadIdx.x == 0) red = 0;
+    __shared__ float part[8];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
     __syncthreads();
-    if ((threadIdx.x & 31) == 0) atomicAdd(&red, acc);
-    __syncthreads();
-    if (threadIdx.x == 0) g[k < H ? H * F + H + k : NW - 1] = red;
+    if (threadIdx.x == 0) {
+        float v = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += part[w];
+        g[k < H ? H * F + H + k : NW - 1] = v;
+    }
 }
 
 __global__ void adam_kernel(float *w, const float *g, float *m, float *v, float lr, float wd, float b1t, float b2t) {
