@@ -70,9 +70,16 @@ struct BParams {
     uint32_t claim;
     uint32_t max_claims;
     uint32_t total_warps;
+    uint32_t latency_sms; // SMs [0, latency_sms) serve only latency-critical phases
     unsigned long long seed;
     unsigned long long timeout_ns;
 };
+
+// A phase is latency-critical when it is small and its instance is deep: such
+// instances advance one short phase at a time, and each claim's latency on a
+// fully loaded SM (several times that on an idle one) is what bounds them.
+constexpr unsigned long long kCriticalStates = 8192;
+constexpr unsigned int kCriticalEpochs = 32;
 
 static __device__ __forceinline__ unsigned long long vload64(const unsigned long long *p) {
     return *(volatile const unsigned long long *)p;
@@ -177,6 +184,12 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(BParams BP) {
     unsigned char *raw = smem + (size_t)(threadIdx.x >> 5) * sizeof(WarpScratch<K128, MODE_PROVISO>);
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    // on a reserved SM every resident warp serves latency-critical phases first,
+    // other phases only when no critical one is claimable; elsewhere warps leave
+    // critical phases to the reserved SMs
+    const bool express = smid < BP.latency_sms;
     uint32_t next = gwarp % BP.count;
     uint32_t claims = 0;
     uint64_t idle_since = 0;
@@ -184,8 +197,10 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(BParams BP) {
         if (vload(&BP.g->done_count) >= BP.count || vload(&BP.g->error)) break;
         if (BP.max_claims && claims >= BP.max_claims) break;
         bool worked = false;
-        for (uint32_t k = 0; k < BP.count && !worked; k++) {
-            uint32_t i = next + k;
+        for (uint32_t k = 0; k < (express ? 2 * BP.count : BP.count) && !worked; k++) {
+            // a reserved SM's warp scans twice: critical phases only, then any phase
+            const bool any = k >= BP.count;
+            uint32_t i = next + (any ? k - BP.count : k);
             if (i >= BP.count) i -= BP.count;
             BInst *I = &BP.inst[i];
             if (vload(&I->ctrl.done)) continue;
@@ -195,6 +210,10 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(BParams BP) {
             BLevel L = read_level(I, e);
             unsigned long long n = L.hi - L.lo;
             if ((t & kCurMask) >= n) continue;
+            if (BP.latency_sms) {
+                const bool critical = n <= kCriticalStates && e >= kCriticalEpochs;
+                if (express ? (!critical && !any) : critical) continue;
+            }
             // level-sized claims (at least the tuned size) keep few-state levels on many warps
             unsigned long long claim = n / ((unsigned long long)BP.total_warps * 4ull);
             claim = claim < BP.claim ? BP.claim : (claim > 4096 ? 4096 : claim);
@@ -310,7 +329,7 @@ namespace {
     } while (0)
 
 struct BatchConfig {
-    int blocks, threads, claim, kernel_iters;
+    int blocks, threads, claim, kernel_iters, latency_sms;
     double load_factor;
 };
 
@@ -490,6 +509,9 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
     BP.max_claims = (uint32_t)std::max(0, cfg.kernel_iters);
     BP.seed = seed;
     BP.timeout_ns = 20ull * 1000 * 1000 * 1000;
+    // only with a full grid: every SM, the reserved ones included, then hosts blocks
+    BP.latency_sms =
+        cfg.blocks > 0 ? 0u : (uint32_t)std::max(0, std::min(cfg.latency_sms, prop.multiProcessorCount / 2));
     smem = (size_t)(cfg.threads / 32) * sizeof(WarpScratch<K128, MODE_PROVISO>);
     BCUDA(cudaFuncSetAttribute((const void *)batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     {
@@ -581,6 +603,7 @@ void gpx_batch_options_init(gpx_batch_options *o) {
     memset(o, 0, sizeof *o);
     o->struct_size = sizeof *o;
     o->seed = 0x243F6A8885A308D3ull;
+    o->latency_sms = -1;
 }
 
 void gpx_batch_job_init(gpx_batch_job *j) {
@@ -605,6 +628,9 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
     cfg.claim = opts->claim > 0 ? opts->claim : 64;
     cfg.kernel_iters = opts->kernel_iters;
     cfg.load_factor = opts->load_factor > 0 ? opts->load_factor : 0.5;
+    // automatic: about a tenth of the SMs (16 of 152 measured best on config 5, with 8
+    // and 24 worse); 0 switches the reservation off
+    cfg.latency_sms = opts->latency_sms >= 0 ? opts->latency_sms : prop.multiProcessorCount / 10 + 1;
     if (cfg.threads % 32 || cfg.threads > 256 || cfg.load_factor > 0.95) return GPX_ERR_INVALID;
     const int max_adm = opts->max_admissions > 0 ? opts->max_admissions : 3;
     gpx_batch_stats st;

@@ -313,6 +313,8 @@ typedef struct {
     double load_factor;     /* table slots = admitted states / load_factor (0 = 0.5) */
     uint64_t seed;
     const gpx_por_model *por_model; /* for jobs with por == 2 (NULL: plain cample) */
+    int32_t latency_sms;    /* SMs that serve the small phases of deep instances (latency-bound) first:
+                               -1 (gpx_batch_options_init) = a tenth of the SMs, 0 = none */
 } gpx_batch_options;
 
 typedef struct {
