@@ -315,22 +315,27 @@ def run_other_workload(args, local):
                     config={"workload": desc, "states_per_step": states // args.steps, "networks": len(nets),
                             "kernel_ms_per_step": kms / args.steps, **extra})
     else:
+        from gpuexplore_gb300 import learned_por
         rng = random.Random(5)
         nets = gen.batch(5, count=args.batch_count)
         models = [lib.Model.from_words(gpf.encode(n)) for n in nets]
+        # the learned cluster proposal for the POR half (outside the timed region):
+        # candidate logs of 200 config-2 seeds, the label and initialisation config 4 selects
+        rows = learned_por.log_candidates(range(1, 201), budget=20_000, sample_every=128, device=local)
+        por_model, _ = learned_por.train(rows, target="succ", device=local, seed=8)
         jobs = []
         for k in range(len(nets)):
             jobs.append({"property": "deadlock" if k % 2 == 0 else "safety",
-                         "por": 1 if (k // 2) % 2 else 0, "cycle_proviso": 1 if (k // 2) % 2 else 0,
+                         "por": 2 if (k // 2) % 2 else 0, "cycle_proviso": 1 if (k // 2) % 2 else 0,
                          "max_states": int(10 ** rng.uniform(3, 7))})
         # the warm-up call autotunes claim size, block size and load factor; timed calls reuse them
         tuned = {}
         for w in range(max(1, args.warmup)):
-            _, st = lib.batch_explore(models, jobs, autotune=1 if w == 0 else 0, **tuned)
+            _, st = lib.batch_explore(models, jobs, autotune=1 if w == 0 else 0, por_model=por_model, **tuned)
             tuned = {"claim": st["claim"], "threads": st["threads"], "load_factor": st["load_factor"]}
         dev, states, p50, p99 = 0.0, 0, [], []
         for _ in range(args.steps):
-            items, st = lib.batch_explore(models, jobs, **tuned)
+            items, st = lib.batch_explore(models, jobs, por_model=por_model, **tuned)
             dev += st["device_ms"]
             states += st["states"]
             p50.append(st["p50_ms"])
@@ -338,7 +343,7 @@ def run_other_workload(args, local):
         line.update(value=states / (dev / 1000.0), ms_per_step=dev / args.steps,
                     config={"workload": f"config-5 batch of {len(nets)} random networks (4-24 procs x 4-32 states), "
                                         "state budgets log-uniform 1e3-1e7, half -d / half -p, half cluster POR with "
-                                        "the cycle proviso, one persistent launch",
+                                        "the learned proposal and the cycle proviso, one persistent launch",
                             "states_per_step": states // args.steps, "p50_ms": statistics.median(p50),
                             "p99_ms": statistics.median(p99), "claim": st["claim"], "threads": st["threads"],
                             "load_factor": st["load_factor"], "tune_ms": st["tune_ms"],

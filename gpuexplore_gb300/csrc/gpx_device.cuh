@@ -403,6 +403,7 @@ template <class K, int MODE> struct WarpScratch {
     uint32_t cl0[kPor];          // per pair: static POR cluster
     uint32_t clo[kPor];          // per pair: cluster closure
     uint32_t nw[kPor];           // per pair: successors not yet visited (decide pass, for the log)
+    uint16_t cand[kPor];         // learned proposal / log: the pairs whose closure is scored
     uint32_t prov[32], sel[32], best[32], vmask[32];
     unsigned long long lbest[32]; // learned proposal: (sortable score, popcount, process)
 };
@@ -904,14 +905,30 @@ template <class K, int MODE> struct Explorer {
         const bool learn = P.learned && P.por_model;
         const bool logging = (MODE == MODE_PROVISO) && P.log && prefix;
         if (learn || logging) {
-            for (uint32_t i = lane; i < npairs; i += 32) {
-                uint32_t g = i / n, p = i - g * n;
-                if (!(ws.vmask[g] >> p & 1u)) continue;
-                uint32_t C = ws.clo[i];
-                bool first = true; // one entry per distinct closure of the state
-                for (uint32_t q = 0; q < p; q++)
-                    if ((ws.vmask[g] >> q & 1u) && ws.clo[g * n + q] == C) first = false;
-                if (!first) continue;
+            // compact the candidates (one per distinct valid closure of a state) so
+            // that every lane of a round scores one: a round costs a whole MLP
+            uint32_t ncand = 0;
+            for (uint32_t base = 0; base < npairs; base += 32) {
+                const uint32_t i = base + lane;
+                bool cand = false;
+                if (i < npairs) {
+                    const uint32_t g = i / n, p = i - g * n;
+                    if (ws.vmask[g] >> p & 1u) {
+                        const uint32_t C = ws.clo[i];
+                        cand = true;
+                        for (uint32_t q = 0; q < p; q++)
+                            if ((ws.vmask[g] >> q & 1u) && ws.clo[g * n + q] == C) cand = false;
+                    }
+                }
+                const uint32_t m = __ballot_sync(kFull, cand);
+                if (cand) ws.cand[ncand + __popc(m & lanemask_lt)] = (uint16_t)i;
+                ncand += __popc(m);
+            }
+            __syncwarp();
+            for (uint32_t c = lane; c < ncand; c += 32) {
+                const uint32_t i = ws.cand[c];
+                const uint32_t g = i / n, p = i - g * n;
+                const uint32_t C = ws.clo[i];
                 uint32_t xw[10], succ = 0;
                 cluster_features(g, C, prefix, xw, succ);
                 if (learn) {
