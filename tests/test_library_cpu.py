@@ -81,6 +81,8 @@ def test_cli_surface(built, tmp_path):
     assert r.returncode == 1 and "No input network given" in r.stderr
     r = subprocess.run([cli, "--help"], capture_output=True, text=True)
     assert r.returncode == 0 and "Usage: gpuexplore" in r.stdout
+    for flag in ("--por", "--cycle-proviso", "--ample", "--stubborn", "--por-model", "--dump", "-k", "-q"):
+        assert flag in r.stdout, flag
     r = subprocess.run([cli, str(tmp_path / "x"), "-z"], capture_output=True, text=True)
     assert r.returncode == 1 and "unrecognized option -z" in r.stderr
     r = subprocess.run([cli, str(tmp_path / "x")], capture_output=True, text=True)
@@ -89,3 +91,23 @@ def test_cli_surface(built, tmp_path):
     r = subprocess.run([cli, str(tmp_path / "ring"), "-p"], capture_output=True, text=True)
     assert "Property to check is not a liveness property" in r.stdout
     assert "nr of procs: 8" in r.stdout and "statevector offset 8: 24" in r.stdout
+
+
+def test_option_validation_before_device(built, tmp_path):
+    """Malformed options are refused before any device is touched (works without a GPU)."""
+    from gpuexplore_gb300 import lib
+    p = tmp_path / "m.gpf"
+    gpf.write(gen.ring(1), str(p))
+    for bad in (dict(por=5), dict(por=-1), dict(bucket_bytes=64)):
+        r = lib.explore(str(p), check=False, **bad)
+        assert r["rc"] == 6, bad  # GPX_ERR_INVALID
+
+
+def test_option_defaults(built):
+    from gpuexplore_gb300 import lib
+    o = lib.options()
+    assert o.launch_graph == 1 and o.por == 0 and o.kernel_iters == 0 and o.bucket_bytes == 0
+    L = lib.load()
+    b = lib.BatchOptions()
+    L.gpx_batch_options_init(lib.C.byref(b))
+    assert b.latency_sms == -1 and b.struct_size == lib.C.sizeof(lib.BatchOptions)
