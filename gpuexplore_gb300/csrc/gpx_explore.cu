@@ -416,6 +416,8 @@ struct gpx_explorer {
     unsigned long long *h_levels = nullptr;  // pinned: the first kGraphLevels level counts
     unsigned long long *h_scalar = nullptr;  // pinned: set hash, table count
     LiveScratch live;                        // accepting-cycle check (liveness)
+    size_t saved_fetch = 0;                  // the context's L2 fetch granularity limit before the first run
+    bool fetch_saved = false;
 };
 
 namespace {
@@ -773,6 +775,10 @@ void gpx_model_free(gpx_model *m) { delete m; }
 
 void gpx_explorer_destroy(gpx_explorer *ex) {
     if (!ex) return;
+    if (ex->fetch_saved) {
+        cudaSetDevice(ex->o.device);
+        cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, ex->saved_fetch);
+    }
     destroy_graph(ex);
     live_free(&ex->live);
     if (ex->st_body) cudaStreamDestroy(ex->st_body);
@@ -883,17 +889,15 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     const unsigned int first_phase = ex->mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND;
     // Hash probes are random 32-byte reads: ask L2 to fetch no more than a sector
     // per miss (unset, a miss fills 128 bytes; the request rate is the same either
-    // way, the DRAM traffic is not).  The caller's limit is restored afterwards.
-    size_t saved_fetch = 0;
-    bool restore_fetch = cudaDeviceGetLimit(&saved_fetch, cudaLimitMaxL2FetchGranularity) == cudaSuccess &&
-                         cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, 32) == cudaSuccess;
-    struct FetchRestore {
-        bool on;
-        size_t v;
-        ~FetchRestore() {
-            if (on) cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, v);
-        }
-    } fetch_restore{restore_fetch, saved_fetch};
+    // way, the DRAM traffic is not).  Setting the limit waits for the device (a few
+    // hundred microseconds), so it is set only when it differs, and the caller's
+    // value comes back when the explorer is destroyed.
+    size_t cur_fetch = 0;
+    if (cudaDeviceGetLimit(&cur_fetch, cudaLimitMaxL2FetchGranularity) == cudaSuccess && cur_fetch != 32 &&
+        cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, 32) == cudaSuccess && !ex->fetch_saved) {
+        ex->saved_fetch = cur_fetch;
+        ex->fetch_saved = true;
+    }
     unsigned long long launches = 0;
     float kernel_ms = 0, setup_ms = 0, total_ms = 0;
     // -v prints between launches, so it keeps the host loop
