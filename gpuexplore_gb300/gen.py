@@ -256,14 +256,17 @@ def _sync_pool(rng: random.Random, procs: List[int], nactions: int,
 def random_network(seed: int, nprocs: int = 16, states: Tuple[int, int] = (8, 32),
                    outdeg: Tuple[int, int] = (1, 4), sync_frac: float = 0.2,
                    parties: Tuple[int, int] = (2, 3), safety: bool = True,
-                   nactions: Optional[int] = None) -> Network:
-    """Random network: `nprocs` processes with U[states] local states, out-degree
-    U[outdeg] per state, each transition synchronising with probability
-    `sync_frac` (an action shared by 2-3 seeded processes), otherwise local.
-    With `safety`, a monitor over a seeded pair of error local states is
+                   nactions: Optional[int] = None, nstates: Optional[List[int]] = None) -> Network:
+    """Random network: `nprocs` processes with U[states] local states (or exactly
+    `nstates`), out-degree U[outdeg] per state, each transition synchronising with
+    probability `sync_frac` (an action shared by 2-3 seeded processes), otherwise
+    local.  With `safety`, a monitor over a seeded pair of error local states is
     appended (see :func:`add_safety_monitor`), giving nprocs+1 processes."""
     rng = random.Random(seed)
     nst = [rng.randint(states[0], states[1]) for _ in range(nprocs)]
+    if nstates is not None:
+        nst = list(nstates)
+        nprocs = len(nst)
     net = _empty(nst)
     na = nactions if nactions is not None else 2 * nprocs
     rules, acts_of = _sync_pool(rng, list(range(nprocs)), na, parties)

@@ -105,3 +105,21 @@ def test_high_load_bounded_eviction(gpu, tmp_path, slots_per_state):
     assert g["table_count"] == g["states"]  # every state stored exactly once
     if slots_per_state < 1.1:
         assert g["evictions"] > 0
+
+
+# exact key-width boundaries: 31/32 bits (32- vs 64-bit slots), 63/64 (64- vs
+# 128-bit), and 126 bits over 31 processes (the widest vector and the process limit)
+WIDTHS = {31: [15] * 7 + [7], 32: [15] * 8, 63: [15] * 15 + [7], 64: [15] * 16, 126: [31, 31] + [15] * 29}
+
+
+@pytest.mark.parametrize("bits", sorted(WIDTHS))
+@pytest.mark.parametrize("flags", ["deadlock", "por_proviso", "stubborn_deadlock"])
+def test_width_boundaries(gpu, tmp_path, bits, flags):
+    net = gen.random_network(7, nstates=WIDTHS[bits], outdeg=(1, 2), safety=False)
+    assert net.firstbit()[-1] == bits
+    path = write_net(net, tmp_path, f"w{bits}")
+    cli, kw = FLAGS[flags]
+    o = oracle(path, cli, max_states=60_000)
+    g = _gpu(gpu, path, kw, max_states=60_000)
+    _same(o, g)
+    assert g["slot_bytes"] == (4 if bits <= 31 else (8 if bits <= 63 else 16))
