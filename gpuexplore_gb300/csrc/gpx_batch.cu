@@ -282,7 +282,7 @@ __global__ void batch_init_kernel(BParams BP, int first_launch) {
     if (i == 0 && first_launch) BP.g->start_ns = globaltimer();
     if (i >= BP.count) return;
     BInst *I = &BP.inst[i];
-    K128 key = KT<K128>::initial();
+    K128 key = KT<K128>::initial(0);
     unsigned int probes = 0;
     find_or_insert<K128>(I->table, I->nbuckets, key, KT<K128>::hash(key, BP.seed), probes);
     I->store[0] = key;

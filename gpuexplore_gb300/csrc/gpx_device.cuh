@@ -48,6 +48,7 @@ struct alignas(128) Ctrl {
     unsigned int phase;             // Phase
     unsigned int launch_levels;     // levels closed in this launch
     unsigned int timeout_at;        // where a bounded wait gave up (diagnostics)
+    unsigned int tag;               // generation of this run's keys (tagged 128-bit slots; else 0)
     unsigned long long overflow_count; // keys whose probe sequence was full during this level
     unsigned long long evictions;      // keys displaced to make room
     unsigned long long launches;       // exploration launches of a graph-driven run
@@ -87,6 +88,8 @@ struct Params {
     gpx_por_log_row *log;
     unsigned long long *log_count;
     unsigned long long log_cap;
+    // the run's key generation, written by the host before the run (null: 0)
+    const unsigned long long *gen;
 };
 
 // ------------------------------------------------------------- device helpers
@@ -123,10 +126,11 @@ template <class K> struct KT;
 
 template <> struct KT<K32> {
     static constexpr int kSlots = 8; // 32-byte bucket
-    __device__ static K32 initial() { return {0x80000000u}; }
+    __device__ static K32 initial(uint32_t) { return {0x80000000u}; }
+    __device__ static uint32_t tag_of(const K32 &) { return 0; }
     __device__ static bool eq(const K32 &a, const K32 &b) { return a.v == b.v; }
-    __device__ static bool empty(const K32 &a) { return a.v == 0; }
-    __device__ static bool torn(const K32 &) { return false; }
+    __device__ static bool empty(const K32 &a, uint32_t) { return a.v == 0; }
+    __device__ static bool torn(const K32 &, uint32_t) { return false; }
     __device__ static uint32_t get(const K32 &k, uint32_t f, uint32_t w) { return (k.v >> f) & (uint32_t)lmask(w); }
     __device__ static void set(K32 &k, uint32_t f, uint32_t w, uint32_t x) {
         uint32_t m = (uint32_t)lmask(w) << f;
@@ -149,10 +153,11 @@ template <> struct KT<K32> {
 
 template <> struct KT<K64> {
     static constexpr int kSlots = 4; // 32-byte bucket
-    __device__ static K64 initial() { return {0x8000000000000000ull}; }
+    __device__ static K64 initial(uint32_t) { return {0x8000000000000000ull}; }
+    __device__ static uint32_t tag_of(const K64 &) { return 0; }
     __device__ static bool eq(const K64 &a, const K64 &b) { return a.v == b.v; }
-    __device__ static bool empty(const K64 &a) { return a.v == 0; }
-    __device__ static bool torn(const K64 &) { return false; }
+    __device__ static bool empty(const K64 &a, uint32_t) { return a.v == 0; }
+    __device__ static bool torn(const K64 &, uint32_t) { return false; }
     __device__ static uint32_t get(const K64 &k, uint32_t f, uint32_t w) { return (uint32_t)((k.v >> f) & lmask(w)); }
     __device__ static void set(K64 &k, uint32_t f, uint32_t w, uint32_t x) {
         unsigned long long m = lmask(w) << f;
@@ -175,6 +180,62 @@ template <> struct KT<K64> {
     }
 };
 
+// Shared by the two 128-bit slot forms: the state vector is split into a low
+// part of S bits (in the low 64-bit half) and the rest (in the high half).
+template <uint32_t S> struct Split128 {
+    __device__ static uint32_t get(unsigned long long lo, unsigned long long hi, uint32_t f, uint32_t w) {
+        if (f + w <= S) return (uint32_t)((lo >> f) & lmask(w));
+        if (f >= S) return (uint32_t)((hi >> (f - S)) & lmask(w));
+        uint32_t nlo = S - f;
+        return (uint32_t)(((lo >> f) & lmask(nlo)) | ((hi & lmask(w - nlo)) << nlo));
+    }
+    __device__ static void set(unsigned long long &lo, unsigned long long &hi, uint32_t f, uint32_t w, uint32_t x) {
+        if (f + w <= S) {
+            unsigned long long m = lmask(w) << f;
+            lo = (lo & ~m) | (((unsigned long long)x << f) & m);
+        } else if (f >= S) {
+            unsigned long long m = lmask(w) << (f - S);
+            hi = (hi & ~m) | (((unsigned long long)x << (f - S)) & m);
+        } else {
+            uint32_t nlo = S - f;
+            unsigned long long ml = lmask(nlo) << f, mh = lmask(w - nlo);
+            lo = (lo & ~ml) | (((unsigned long long)x << f) & ml);
+            hi = (hi & ~mh) | (((unsigned long long)x >> nlo) & mh);
+        }
+    }
+    // the state vector as 32-bit words (lo and hi hold state bits only)
+    __device__ static void words(unsigned long long lo, unsigned long long hi, uint32_t (&w)[4]) {
+        w[0] = (uint32_t)lo;
+        w[1] = (uint32_t)(lo >> 32) | (uint32_t)(hi << (S - 32));
+        w[2] = (uint32_t)(hi >> (64 - S));
+        w[3] = (uint32_t)(hi >> (96 - S));
+    }
+};
+
+static __device__ __forceinline__ void cas128(void *p, unsigned long long clo, unsigned long long chi,
+                                              unsigned long long vlo, unsigned long long vhi,
+                                              unsigned long long &olo, unsigned long long &ohi) {
+    asm volatile(
+        "{\n\t.reg .b128 c, v, o;\n\t"
+        "mov.b128 c, {%2, %3};\n\t"
+        "mov.b128 v, {%4, %5};\n\t"
+        "atom.global.cas.b128 o, [%6], c, v;\n\t"
+        "mov.b128 {%0, %1}, o;\n\t}"
+        : "=l"(olo), "=l"(ohi)
+        : "l"(clo), "l"(chi), "l"(vlo), "l"(vhi), "l"(p)
+        : "memory");
+}
+
+static __device__ __forceinline__ void bucket128(const void *b, unsigned long long (&lo)[2],
+                                                 unsigned long long (&hi)[2]) {
+    uint32_t w[8];
+    ld256_cg(b, w);
+    lo[0] = (unsigned long long)w[0] | ((unsigned long long)w[1] << 32);
+    hi[0] = (unsigned long long)w[2] | ((unsigned long long)w[3] << 32);
+    lo[1] = (unsigned long long)w[4] | ((unsigned long long)w[5] << 32);
+    hi[1] = (unsigned long long)w[6] | ((unsigned long long)w[7] << 32);
+}
+
 // 128-bit slots hold 63 state bits in each 64-bit half (bit 63 of both halves
 // is the occupancy marker).  Each half is read atomically, so a slot caught in
 // the middle of its insertion shows exactly one zero half ("torn"); such a slot
@@ -182,62 +243,73 @@ template <> struct KT<K64> {
 template <> struct KT<K128> {
     static constexpr int kSlots = 2; // 32-byte bucket
     static constexpr unsigned long long kOcc = 0x8000000000000000ull;
-    __device__ static K128 initial() { return {kOcc, kOcc}; }
+    using Sp = Split128<63>;
+    __device__ static K128 initial(uint32_t) { return {kOcc, kOcc}; }
+    __device__ static uint32_t tag_of(const K128 &) { return 0; }
     __device__ static bool eq(const K128 &a, const K128 &b) { return a.lo == b.lo && a.hi == b.hi; }
-    __device__ static bool empty(const K128 &a) { return (a.lo | a.hi) == 0; }
-    __device__ static bool torn(const K128 &a) { return (a.lo == 0) != (a.hi == 0); }
-    __device__ static uint32_t get(const K128 &k, uint32_t f, uint32_t w) {
-        if (f + w <= 63) return (uint32_t)((k.lo >> f) & lmask(w));
-        if (f >= 63) return (uint32_t)((k.hi >> (f - 63)) & lmask(w));
-        uint32_t nlo = 63 - f;
-        return (uint32_t)(((k.lo >> f) & lmask(nlo)) | ((k.hi & lmask(w - nlo)) << nlo));
-    }
-    __device__ static void set(K128 &k, uint32_t f, uint32_t w, uint32_t x) {
-        if (f + w <= 63) {
-            unsigned long long m = lmask(w) << f;
-            k.lo = (k.lo & ~m) | (((unsigned long long)x << f) & m);
-        } else if (f >= 63) {
-            unsigned long long m = lmask(w) << (f - 63);
-            k.hi = (k.hi & ~m) | (((unsigned long long)x << (f - 63)) & m);
-        } else {
-            uint32_t nlo = 63 - f;
-            unsigned long long ml = lmask(nlo) << f, mh = lmask(w - nlo);
-            k.lo = (k.lo & ~ml) | (((unsigned long long)x << f) & ml);
-            k.hi = (k.hi & ~mh) | (((unsigned long long)x >> nlo) & mh);
-        }
-    }
+    __device__ static bool empty(const K128 &a, uint32_t) { return (a.lo | a.hi) == 0; }
+    __device__ static bool torn(const K128 &a, uint32_t) { return (a.lo == 0) != (a.hi == 0); }
+    __device__ static uint32_t get(const K128 &k, uint32_t f, uint32_t w) { return Sp::get(k.lo, k.hi, f, w); }
+    __device__ static void set(K128 &k, uint32_t f, uint32_t w, uint32_t x) { Sp::set(k.lo, k.hi, f, w, x); }
     __device__ static uint64_t hash(const K128 &k, uint64_t seed) { return mix64(k.lo ^ mix64(k.hi ^ seed)); }
     __device__ static K128 cas(K128 *p, K128 cmp, K128 val) {
-        unsigned long long olo, ohi;
-        asm volatile(
-            "{\n\t.reg .b128 c, v, o;\n\t"
-            "mov.b128 c, {%2, %3};\n\t"
-            "mov.b128 v, {%4, %5};\n\t"
-            "atom.global.cas.b128 o, [%6], c, v;\n\t"
-            "mov.b128 {%0, %1}, o;\n\t}"
-            : "=l"(olo), "=l"(ohi)
-            : "l"(cmp.lo), "l"(cmp.hi), "l"(val.lo), "l"(val.hi), "l"(p)
-            : "memory");
-        return {olo, ohi};
+        K128 o;
+        cas128(p, cmp.lo, cmp.hi, val.lo, val.hi, o.lo, o.hi);
+        return o;
     }
     __device__ static void bucket(const K128 *b, K128 (&s)[kSlots]) {
-        uint32_t w[8];
-        ld256_cg(b, w);
-        s[0].lo = (unsigned long long)w[0] | ((unsigned long long)w[1] << 32);
-        s[0].hi = (unsigned long long)w[2] | ((unsigned long long)w[3] << 32);
-        s[1].lo = (unsigned long long)w[4] | ((unsigned long long)w[5] << 32);
-        s[1].hi = (unsigned long long)w[6] | ((unsigned long long)w[7] << 32);
+        unsigned long long lo[2], hi[2];
+        bucket128(b, lo, hi);
+        s[0] = {lo[0], hi[0]};
+        s[1] = {lo[1], hi[1]};
     }
-    __device__ static K128 load(const K128 *p) {
-        return {__ldcg(&p->lo), __ldcg(&p->hi)};
+    __device__ static K128 load(const K128 *p) { return {__ldcg(&p->lo), __ldcg(&p->hi)}; }
+    __device__ static void words(const K128 &k, uint32_t (&w)[4]) { Sp::words(k.lo & ~kOcc, k.hi & ~kOcc, w); }
+};
+
+// 128-bit slots of a reusable table: 56 state bits in each 64-bit half and the
+// run's generation (1..255) in the top byte of both halves.  A half carrying
+// another generation -- or zero -- is free, so a new run needs no table clear:
+// the table is zeroed on its first run and once every 255 runs.  During a run
+// a slot still changes once, from free to a key of the run, by a full-slot CAS
+// against the free contents it was read with.  Each half is read atomically, so
+// a slot caught in the middle of its insertion shows exactly one half of the
+// current generation ("torn") and is re-read with an atomic before it is judged.
+// Keys carry the generation, and successors inherit it from their source state.
+struct __align__(16) K128G { unsigned long long lo, hi; };
+
+template <> struct KT<K128G> {
+    static constexpr int kSlots = 2; // 32-byte bucket
+    static constexpr uint32_t kStateBits = 56;
+    static constexpr unsigned long long kMask = (1ull << kStateBits) - 1ull;
+    using Sp = Split128<kStateBits>;
+    __device__ static bool cur(unsigned long long h, uint32_t tag) { return (uint32_t)(h >> kStateBits) == tag; }
+    __device__ static K128G initial(uint32_t tag) {
+        const unsigned long long t = (unsigned long long)tag << kStateBits;
+        return {t, t};
     }
-    __device__ static void words(const K128 &k, uint32_t (&w)[4]) {
-        unsigned long long lo = k.lo & ~kOcc, hi = k.hi & ~kOcc;
-        w[0] = (uint32_t)lo;
-        w[1] = (uint32_t)(lo >> 32) | (uint32_t)((hi & 1ull) << 31);
-        w[2] = (uint32_t)(hi >> 1);
-        w[3] = (uint32_t)(hi >> 33);
+    __device__ static uint32_t tag_of(const K128G &k) { return (uint32_t)(k.lo >> kStateBits); }
+    __device__ static bool eq(const K128G &a, const K128G &b) { return a.lo == b.lo && a.hi == b.hi; }
+    __device__ static bool empty(const K128G &a, uint32_t tag) { return !cur(a.lo, tag) && !cur(a.hi, tag); }
+    __device__ static bool torn(const K128G &a, uint32_t tag) { return cur(a.lo, tag) != cur(a.hi, tag); }
+    __device__ static uint32_t get(const K128G &k, uint32_t f, uint32_t w) { return Sp::get(k.lo, k.hi, f, w); }
+    __device__ static void set(K128G &k, uint32_t f, uint32_t w, uint32_t x) { Sp::set(k.lo, k.hi, f, w, x); }
+    __device__ static uint64_t hash(const K128G &k, uint64_t seed) {
+        return mix64((k.lo & kMask) ^ mix64((k.hi & kMask) ^ seed));
     }
+    __device__ static K128G cas(K128G *p, K128G cmp, K128G val) {
+        K128G o;
+        cas128(p, cmp.lo, cmp.hi, val.lo, val.hi, o.lo, o.hi);
+        return o;
+    }
+    __device__ static void bucket(const K128G *b, K128G (&s)[kSlots]) {
+        unsigned long long lo[2], hi[2];
+        bucket128(b, lo, hi);
+        s[0] = {lo[0], hi[0]};
+        s[1] = {lo[1], hi[1]};
+    }
+    __device__ static K128G load(const K128G *p) { return {__ldcg(&p->lo), __ldcg(&p->hi)}; }
+    __device__ static void words(const K128G &k, uint32_t (&w)[4]) { Sp::words(k.lo & kMask, k.hi & kMask, w); }
 };
 
 // Probe sequence of a key: 32-byte buckets visited in pairs -- a bucket, then
@@ -254,12 +326,13 @@ static __device__ __forceinline__ unsigned long long bucket_of(uint64_t h, int i
 // it, 2 if every probed bucket was full.  Slots go from empty to a key exactly
 // once during a level (keys move only in place_evicting, when no other thread
 // inserts); every caller scans the same probe sequence and claims the first
-// empty slot it sees with a full-key CAS, so two insertions of one key always
-// meet in the same slot and exactly one wins.
+// empty slot it sees with a full-key CAS against the contents it read, so two
+// insertions of one key always meet in the same slot and exactly one wins.
 template <class K>
 __device__ __forceinline__ int find_or_insert(K *table, unsigned long long nb, const K &key, uint64_t h,
                                               unsigned int &probes) {
     constexpr int S = KT<K>::kSlots;
+    const uint32_t tag = KT<K>::tag_of(key);
     for (int i = 0; i < kMaxProbe; i++) {
         K *b = table + bucket_of(h, i, nb) * S;
         K s[S];
@@ -270,11 +343,10 @@ __device__ __forceinline__ int find_or_insert(K *table, unsigned long long nb, c
             if (KT<K>::eq(s[j], key)) return 0;
 #pragma unroll
         for (int j = 0; j < S; j++) {
-            if (KT<K>::empty(s[j]) || KT<K>::torn(s[j])) {
-                K zero;
-                memset(&zero, 0, sizeof zero);
-                K old = KT<K>::cas(b + j, zero, key);
-                if (KT<K>::empty(old)) return 1;
+            // a torn slot is being filled: the CAS fails and returns the key
+            if (KT<K>::empty(s[j], tag) || KT<K>::torn(s[j], tag)) {
+                K old = KT<K>::cas(b + j, s[j], key);
+                if (KT<K>::eq(old, s[j])) return 1;
                 if (KT<K>::eq(old, key)) return 0;
             }
         }
@@ -293,12 +365,13 @@ __device__ int place_evicting(K *table, unsigned long long nb, const K &key, uns
                               unsigned long long &evictions) {
     constexpr int S = KT<K>::kSlots;
     const uint64_t h = KT<K>::hash(key, seed);
+    const uint32_t tag = KT<K>::tag_of(key);
     for (int i = 0; i < kMaxProbe; i++) { // placed meanwhile (a duplicate overflow entry) or room after all
         K *b = table + bucket_of(h, i, nb) * S;
         for (int j = 0; j < S; j++) {
             K v = KT<K>::load(b + j);
             if (KT<K>::eq(v, key)) return 0;
-            if (KT<K>::empty(v)) {
+            if (KT<K>::empty(v, tag)) {
                 b[j] = key;
                 return 1;
             }
@@ -316,7 +389,7 @@ __device__ int place_evicting(K *table, unsigned long long nb, const K &key, uns
             for (int q = iv + 1; iv >= 0 && q < kMaxProbe; q++) {
                 K *bv = table + bucket_of(hv, q, nb) * S;
                 for (int jj = 0; jj < S; jj++) {
-                    if (KT<K>::empty(KT<K>::load(bv + jj))) {
+                    if (KT<K>::empty(KT<K>::load(bv + jj), tag)) {
                         bv[jj] = v;
                         b[j] = key;
                         evictions++;
@@ -368,6 +441,7 @@ template <class K>
 __device__ __forceinline__ bool find_key(K *table, unsigned long long nb, const K &key, uint64_t h,
                                          unsigned int &probes) {
     constexpr int S = KT<K>::kSlots;
+    const uint32_t tag = KT<K>::tag_of(key);
     for (int i = 0; i < kMaxProbe; i++) {
         K *b = table + bucket_of(h, i, nb) * S;
         K s[S];
@@ -376,13 +450,9 @@ __device__ __forceinline__ bool find_key(K *table, unsigned long long nb, const 
 #pragma unroll
         for (int j = 0; j < S; j++) {
             K v = s[j];
-            if (KT<K>::torn(v)) {
-                K zero;
-                memset(&zero, 0, sizeof zero);
-                v = KT<K>::cas(b + j, zero, zero); // atomic re-read; writes nothing new
-            }
+            if (KT<K>::torn(v, tag)) v = KT<K>::cas(b + j, v, v); // atomic re-read; the slot is complete
             if (KT<K>::eq(v, key)) return true;
-            if (KT<K>::empty(v)) return false;
+            if (KT<K>::empty(v, tag)) return false;
         }
     }
     return false;

@@ -216,7 +216,8 @@ template <class K> __global__ void init_kernel(Params P, unsigned int first_phas
     c->nlevels = 1;
     c->claim = 1;
     c->phase = first_phase;
-    K key = KT<K>::initial();
+    c->tag = P.gen ? (unsigned int)*P.gen : 0u;
+    K key = KT<K>::initial(c->tag);
     unsigned int probes = 0;
     find_or_insert<K>((K *)P.table, P.nbuckets, key, KT<K>::hash(key, P.seed), probes);
     ((K *)P.store)[0] = key;
@@ -268,13 +269,16 @@ __global__ void set_hash_kernel(const K *store, unsigned long long count, const 
     if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
 }
 
-// Occupied slots of the table (count_states, GPUexplore.cu:687-704).
-template <class K> __global__ void count_kernel(const K *table, unsigned long long slots, unsigned long long *out) {
+// Occupied slots of the table (count_states, GPUexplore.cu:687-704); slots of
+// another generation are free.
+template <class K>
+__global__ void count_kernel(const K *table, unsigned long long slots, const Ctrl *c, unsigned long long *out) {
+    const uint32_t tag = c->tag;
     unsigned long long acc = 0;
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < slots;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         K k = KT<K>::load(table + i);
-        acc += KT<K>::empty(k) ? 0 : 1;
+        acc += KT<K>::empty(k, tag) ? 0 : 1;
     }
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
@@ -316,7 +320,8 @@ struct KernelSet {
     void (*set_hash)(cudaStream_t, int blocks, const void *store, unsigned long long count,
                      const unsigned long long *count_dev, unsigned long long cap, uint32_t words,
                      unsigned long long *out);
-    void (*count)(cudaStream_t, int blocks, const void *table, unsigned long long slots, unsigned long long *out);
+    void (*count)(cudaStream_t, int blocks, const void *table, unsigned long long slots, const Ctrl *c,
+                  unsigned long long *out);
     size_t scratch_bytes[3];
     uint32_t slot_bytes, bucket_slots;
 };
@@ -329,8 +334,9 @@ void launch_set_hash(cudaStream_t st, int blocks, const void *store, unsigned lo
 }
 
 template <class K>
-void launch_count(cudaStream_t st, int blocks, const void *table, unsigned long long slots, unsigned long long *out) {
-    count_kernel<K><<<blocks, 256, 0, st>>>((const K *)table, slots, out);
+void launch_count(cudaStream_t st, int blocks, const void *table, unsigned long long slots, const Ctrl *c,
+                  unsigned long long *out) {
+    count_kernel<K><<<blocks, 256, 0, st>>>((const K *)table, slots, c, out);
 }
 
 template <class K> KernelSet kernels_for() {
@@ -376,7 +382,7 @@ constexpr uint32_t kGraphLevels = 4096; // level counts read back by the graph i
 struct gpx_explorer {
     gpx_options o;
     gpx_model model;
-    int kind = 0; // 0: 32-bit, 1: 64-bit, 2: 128-bit slots
+    int kind = 0; // 0: 32-bit, 1: 64-bit, 2: 128-bit, 3: 128-bit slots with a run generation
     KernelSet ks;
     int mode = MODE_PLAIN;
     int property = GPX_PROP_NONE;
@@ -418,6 +424,10 @@ struct gpx_explorer {
     LiveScratch live;                        // accepting-cycle check (liveness)
     size_t saved_fetch = 0;                  // the context's L2 fetch granularity limit before the first run
     bool fetch_saved = false;
+    // tagged slots (kind 3): generation of the table's newest keys (0: contents
+    // unknown, clear before the next run), and its pinned source for the device
+    unsigned int gen = 0;
+    unsigned long long *h_gen = nullptr;
 };
 
 namespace {
@@ -425,10 +435,21 @@ namespace {
 // gpx_options.por: 1 cample, 2 cample with the learned proposal, 3 ample, 4 stubborn
 uint32_t por_kind_of(int por) { return por == 3 ? POR_AMPLE : (por == 4 ? POR_STUBBORN : POR_CAMPLE); }
 
-int select_kind(uint32_t state_bits) {
+// Slot form for a state width.  A table the explorer keeps across runs takes
+// the generation-tagged form when the state fits its 112 bits.
+int select_kind(uint32_t state_bits, bool reusable) {
     if (state_bits <= 31) return 0;
     if (state_bits <= 63) return 1;
-    return 2;
+    return (reusable && state_bits <= 112) ? 3 : 2;
+}
+
+KernelSet kernels_of(int kind) {
+    switch (kind) {
+    case 0: return kernels_for<K32>();
+    case 1: return kernels_for<K64>();
+    case 2: return kernels_for<K128>();
+    default: return kernels_for<K128G>();
+    }
 }
 
 int load_text(const std::string &path, gpx_model **out) {
@@ -509,6 +530,7 @@ Params make_params(gpx_explorer *ex) {
     P.learned = (ex->o.por == 2 && ex->have_por_model) ? 1u : 0u;
     P.por_kind = por_kind_of(ex->o.por);
     P.por_model = ex->have_por_model ? ex->d_por_model : nullptr;
+    P.gen = ex->d_scalar + 2;
     if (ex->d_log && ex->log_cap && ex->mode == MODE_PROVISO) {
         P.log = ex->d_log;
         P.log_count = ex->d_log_count;
@@ -544,8 +566,9 @@ GraphKey graph_key(const gpx_explorer *ex, const Params &P, unsigned int first_p
     return k;
 }
 
-// Record one run into a graph on ex->st:
-//   reset table + init -> while (more) { exploration launch; relaunch_kernel } -> set hash -> read-back
+// Record one run into a graph on ex->st (the table reset and the generation
+// upload come before it on the stream):
+//   init -> while (more) { exploration launch; relaunch_kernel } -> set hash -> read-back
 // The loop's condition is set on the device by relaunch_kernel, so a -k run
 // needs no host round trip between launches.
 cudaError_t capture_run(gpx_explorer *ex, const GraphKey &k, cudaGraph_t *out) {
@@ -559,8 +582,6 @@ cudaError_t capture_run(gpx_explorer *ex, const GraphKey &k, cudaGraph_t *out) {
     } while (0)
         Params P = k.P;
         GPX_CAP(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        GPX_CAP(cudaEventRecordWithFlags(ex->ev[0], st, cudaEventRecordExternal));
-        GPX_CAP(cudaMemsetAsync(ex->d_table, 0, ex->table_bytes, st));
         if (k.log_count) GPX_CAP(cudaMemsetAsync(k.log_count, 0, 8, st));
         ex->ks.init<<<1, 32, 0, st>>>(P, k.first_phase);
         GPX_CAP(cudaGetLastError());
@@ -596,7 +617,7 @@ cudaError_t capture_run(gpx_explorer *ex, const GraphKey &k, cudaGraph_t *out) {
         GPX_CAP(cudaMemsetAsync(ex->d_scalar, 0, 16, st));
         int hb = (int)std::max<unsigned long long>(1, std::min<unsigned long long>((ex->store_cap + 255) / 256, 4096));
         ex->ks.set_hash(st, hb, ex->d_store, 0, &ex->d_ctrl->store_count, ex->store_cap, k.key_words, ex->d_scalar);
-        if (k.collect) ex->ks.count(st, count_blocks(ex), ex->d_table, ex->slots, ex->d_scalar + 1);
+        if (k.collect) ex->ks.count(st, count_blocks(ex), ex->d_table, ex->slots, ex->d_ctrl, ex->d_scalar + 1);
         GPX_CAP(cudaGetLastError());
         GPX_CAP(cudaMemcpyAsync(ex->h_ctrl, ex->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));
         GPX_CAP(cudaMemcpyAsync(ex->h_scalar, ex->d_scalar, 16, cudaMemcpyDeviceToHost, st));
@@ -683,8 +704,10 @@ int collect_words(gpx_explorer *ex, unsigned long long count, std::vector<uint32
         words_kernel<K32><<<blocks, 256, 0, ex->st>>>((const K32 *)ex->d_store, count, W, d_words);
     else if (ex->kind == 1)
         words_kernel<K64><<<blocks, 256, 0, ex->st>>>((const K64 *)ex->d_store, count, W, d_words);
-    else
+    else if (ex->kind == 2)
         words_kernel<K128><<<blocks, 256, 0, ex->st>>>((const K128 *)ex->d_store, count, W, d_words);
+    else
+        words_kernel<K128G><<<blocks, 256, 0, ex->st>>>((const K128G *)ex->d_store, count, W, d_words);
     cudaError_t e = cudaMemcpyAsync(out->data(), d_words, count * W * 4, cudaMemcpyDeviceToHost, ex->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ex->st);
     cudaFree(d_words);
@@ -784,6 +807,7 @@ void gpx_explorer_destroy(gpx_explorer *ex) {
     if (ex->st_body) cudaStreamDestroy(ex->st_body);
     if (ex->h_levels) cudaFreeHost(ex->h_levels);
     if (ex->h_scalar) cudaFreeHost(ex->h_scalar);
+    if (ex->h_gen) cudaFreeHost(ex->h_gen);
     if (ex->d_table) cudaFree(ex->d_table);
     if (ex->d_store) cudaFree(ex->d_store);
     if (ex->d_model) cudaFree(ex->d_model);
@@ -820,8 +844,8 @@ int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_exp
         delete ex;
         return GPX_ERR_UNSUPPORTED;
     }
-    ex->kind = select_kind(model->dec.state_bits);
-    ex->ks = ex->kind == 0 ? kernels_for<K32>() : (ex->kind == 1 ? kernels_for<K64>() : kernels_for<K128>());
+    ex->kind = select_kind(model->dec.state_bits, true);
+    ex->ks = kernels_of(ex->kind);
     ex->bits_statevector = model->gpf.bits_statevector + (opts->por ? 1u : 0u);
     int rc = GPX_OK;
     auto fail = [&](int code) {
@@ -860,6 +884,7 @@ int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_exp
     if (cudaMalloc(&ex->d_scalar, 64) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (cudaMalloc(&ex->d_ctrl, sizeof(Ctrl)) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (cudaMallocHost(&ex->h_ctrl, sizeof(Ctrl)) != cudaSuccess) return fail(GPX_ERR_NOMEM);
+    if (cudaMallocHost(&ex->h_gen, 8) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if ((rc = upload_model(ex)) != GPX_OK) return fail(rc);
     if (cudaStreamSynchronize(ex->st) != cudaSuccess) return fail(GPX_ERR_CUDA);
     *out = ex;
@@ -868,11 +893,18 @@ int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_exp
 
 int gpx_explorer_set_model(gpx_explorer *ex, const gpx_model *model) {
     if (!ex || !model) return GPX_ERR_INVALID;
-    if (select_kind(model->dec.state_bits) != ex->kind) return GPX_ERR_INVALID;
+    // the slot size is fixed by the table; the two 128-bit forms interchange
+    const int kind = select_kind(model->dec.state_bits, true);
+    if (kind != ex->kind && !(kind >= 2 && ex->kind >= 2)) return GPX_ERR_INVALID;
     int property = ex->o.property;
     if (property == GPX_PROP_SAFETY && model->gpf.liveness == 1) property = GPX_PROP_LIVENESS;
     if (property == GPX_PROP_LIVENESS && ex->mode != MODE_PLAIN) return GPX_ERR_UNSUPPORTED;
     ex->property = property;
+    if (kind != ex->kind) { // the table's keys are of the other form: clear it before the next run
+        ex->kind = kind;
+        ex->ks = kernels_of(kind);
+        ex->gen = 0;
+    }
     ex->model = *model;
     ex->bits_statevector = model->gpf.bits_statevector + (ex->o.por ? 1u : 0u);
     int rc = configure_launch(ex);
@@ -900,6 +932,19 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     }
     unsigned long long launches = 0;
     float kernel_ms = 0, setup_ms = 0, total_ms = 0;
+    // reset: empty table, empty store, initial state (GPUexplore.cu:2091-2092).
+    // Tagged slots need no clear while the generation counts up: a run's keys
+    // carry its generation and older ones read as free.  The table is zeroed
+    // when its contents are unknown (first run, a failed run, a change of slot
+    // form) and when the 8-bit generation is spent.
+    const bool tagged = ex->kind == 3;
+    const bool clear = !tagged || ex->gen == 0 || ex->gen >= 255;
+    const unsigned int tag = tagged ? (clear ? 1u : ex->gen + 1u) : 0u;
+    ex->gen = 0; // until this run has completed
+    *ex->h_gen = tag;
+    GPX_CUDA(cudaEventRecord(ex->ev[0], ex->st));
+    if (clear) GPX_CUDA(cudaMemsetAsync(ex->d_table, 0, ex->table_bytes, ex->st));
+    GPX_CUDA(cudaMemcpyAsync(ex->d_scalar + 2, ex->h_gen, 8, cudaMemcpyHostToDevice, ex->st));
     // -v prints between launches, so it keeps the host loop
     const bool graph = ex->o.launch_graph && ex->o.verbosity <= 0;
     if (graph) {
@@ -910,9 +955,6 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
         cudaEventElapsedTime(&kernel_ms, ex->ev[1], ex->ev[3]);
         total_ms = kernel_ms;
     } else {
-        // reset: empty table, empty store, initial state (GPUexplore.cu:2091-2092)
-        GPX_CUDA(cudaEventRecord(ex->ev[0], ex->st));
-        GPX_CUDA(cudaMemsetAsync(ex->d_table, 0, ex->table_bytes, ex->st));
         if (ex->d_log_count) GPX_CUDA(cudaMemsetAsync(ex->d_log_count, 0, 8, ex->st));
         ex->ks.init<<<1, 32, 0, ex->st>>>(P, first_phase);
         GPX_CUDA(cudaGetLastError());
@@ -956,6 +998,7 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
         cudaEventElapsedTime(&total_ms, ex->ev[1], ex->ev[3]);
     }
     Ctrl &c = *ex->h_ctrl;
+    ex->gen = tag; // the table holds this run's keys (and older, free ones)
     r->status = c.error ? (int)c.error : GPX_OK;
     r->stopped = (int)c.stop;
     if (c.error) r->stopped = GPX_STOP_ERROR;
@@ -979,6 +1022,9 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     r->slot_bytes = ex->ks.slot_bytes;
     r->blocks = (uint32_t)ex->blocks;
     r->threads = (uint32_t)ex->threads;
+    r->h2d_bytes = 8; // the generation
+    r->table_generation = tag;
+    r->table_cleared = clear ? 1 : 0;
     if (graph) {
         // the graph read back the set hash, the table count and the first kGraphLevels level counts
         const uint32_t head = std::min(c.nlevels, kGraphLevels);
@@ -998,14 +1044,14 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
         int blocks = (int)std::min<unsigned long long>((count + 255) / 256, 4096);
         ex->ks.set_hash(ex->st, std::max(blocks, 1), ex->d_store, count, nullptr, 0, r->key_words, ex->d_scalar);
         if (ex->o.collect_states || ex->o.verbosity >= 2)
-            ex->ks.count(ex->st, count_blocks(ex), ex->d_table, ex->slots, ex->d_scalar + 1);
+            ex->ks.count(ex->st, count_blocks(ex), ex->d_table, ex->slots, ex->d_ctrl, ex->d_scalar + 1);
         GPX_CUDA(cudaGetLastError());
         unsigned long long h[2] = {0, 0};
         GPX_CUDA(cudaMemcpyAsync(h, ex->d_scalar, 16, cudaMemcpyDeviceToHost, ex->st));
         GPX_CUDA(cudaStreamSynchronize(ex->st));
         r->set_hash = h[0];
         r->table_count = h[1];
-        r->h2d_bytes = (launches - 1) * 2 * sizeof(unsigned int); // -k rearm between launches
+        r->h2d_bytes += (launches - 1) * 2 * sizeof(unsigned int); // -k rearm between launches
         r->d2h_bytes = launches * sizeof(Ctrl) + (uint64_t)c.nlevels * 8 + 16;
     }
     if (ex->property == GPX_PROP_LIVENESS && r->status == GPX_OK && r->stopped == GPX_STOP_DONE) {
@@ -1273,8 +1319,8 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     int property = opts->property;
     if (property == GPX_PROP_SAFETY && model->gpf.liveness == 1) property = GPX_PROP_LIVENESS;
     if (property == GPX_PROP_LIVENESS) return GPX_ERR_UNSUPPORTED; // the cycle check needs scratch of its own
-    const int kind = select_kind(model->dec.state_bits);
-    KernelSet ks = kind == 0 ? kernels_for<K32>() : (kind == 1 ? kernels_for<K64>() : kernels_for<K128>());
+    const int kind = select_kind(model->dec.state_bits, false); // the table is cleared on every call
+    KernelSet ks = kernels_of(kind);
 
     // carve the array
     const size_t total = GPX_NOALLOC_SCRATCH_BYTES;
@@ -1404,6 +1450,7 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     r->key_words = model->dec.key_words;
     r->table_slots = P.nbuckets * ks.bucket_slots;
     r->slot_bytes = ks.slot_bytes;
+    r->table_cleared = 1;
     r->blocks = (uint32_t)blocks;
     r->threads = (uint32_t)threads;
     return r->status;

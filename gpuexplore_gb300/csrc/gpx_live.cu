@@ -39,6 +39,7 @@ constexpr uint32_t kInSet = 1u, kMarked = 2u;
 template <class K>
 __device__ unsigned long long find_slot(const K *table, unsigned long long nb, const K &key, uint64_t h) {
     constexpr int S = KT<K>::kSlots;
+    const uint32_t tag = KT<K>::tag_of(key);
     for (int i = 0; i < kMaxProbe; i++) {
         const unsigned long long b = bucket_of(h, i, nb);
         K s[S];
@@ -46,7 +47,7 @@ __device__ unsigned long long find_slot(const K *table, unsigned long long nb, c
 #pragma unroll
         for (int j = 0; j < S; j++) {
             if (KT<K>::eq(s[j], key)) return b * S + j;
-            if (KT<K>::empty(s[j])) return ~0ull;
+            if (KT<K>::empty(s[j], tag)) return ~0ull;
         }
     }
     return ~0ull;
@@ -389,8 +390,11 @@ int live_check(int kind, void *table, unsigned long long nbuckets, unsigned long
     if (kind == 1)
         return run<K64>((const K64 *)table, nbuckets, slots, (const K64 *)store, states, model, seed, st, s,
                         set_states, rounds);
-    return run<K128>((const K128 *)table, nbuckets, slots, (const K128 *)store, states, model, seed, st, s,
-                     set_states, rounds);
+    if (kind == 2)
+        return run<K128>((const K128 *)table, nbuckets, slots, (const K128 *)store, states, model, seed, st, s,
+                         set_states, rounds);
+    return run<K128G>((const K128G *)table, nbuckets, slots, (const K128G *)store, states, model, seed, st, s,
+                      set_states, rounds);
 }
 
 } // namespace gpx

@@ -22,7 +22,8 @@ void live_free(LiveScratch *s);
 // After a complete exploration: does a cycle of the full transition relation
 // pass through a state whose last process is in local state 1?  `table` holds
 // exactly the visited states and `store` lists them (positions 0..states-1;
-// slot width by kind: 0 = 32, 1 = 64, 2 = 128 bits); `model` is the decoded
+// slot form by kind: 0 = 32, 1 = 64, 2 = 128 bits, 3 = 128 bits with a run
+// generation, whose older-generation slots count as free); `model` is the decoded
 // device layout.  On success *set_states is the size of the final candidate set
 // (0: no accepting cycle) and *rounds the frontier rounds.
 int live_check(int kind, void *table, unsigned long long nbuckets, unsigned long long slots, const void *store,

@@ -87,7 +87,7 @@ class Result(C.Structure):
         ("table_slots", C.c_uint64), ("slot_bytes", C.c_uint32), ("blocks", C.c_uint32), ("threads", C.c_uint32),
         ("inserts", C.c_uint64), ("evictions", C.c_uint64),
         ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("live_states", C.c_uint64), ("live_ms", C.c_double),
-        ("live_rounds", C.c_uint64),
+        ("live_rounds", C.c_uint64), ("table_generation", C.c_uint32), ("table_cleared", C.c_int32),
     ]
 
 
@@ -141,6 +141,7 @@ class DeviceInfo(C.Structure):
 
 
 _lib: Optional[C.CDLL] = None
+ABI_VERSION = 3
 
 
 def load(path: str = LIB) -> C.CDLL:
@@ -155,6 +156,8 @@ def load(path: str = LIB) -> C.CDLL:
     lib.gpx_status_string.restype = C.c_char_p
     lib.gpx_status_string.argtypes = [i]
     lib.gpx_abi_version.restype = i
+    if lib.gpx_abi_version() != ABI_VERSION:  # the structures below mirror this version of gpx.h
+        raise RuntimeError(f"libgpx ABI {lib.gpx_abi_version()} != {ABI_VERSION}: rebuild it")
     lib.gpx_device_info_get.argtypes = [i, C.POINTER(DeviceInfo)]
     lib.gpx_options_init.argtypes = [C.POINTER(Options)]
     lib.gpx_options_init.restype = None
@@ -269,6 +272,7 @@ def _result_dict(r: Result) -> Dict:
         "inserts": int(r.inserts), "evictions": int(r.evictions),
         "h2d_bytes": int(r.h2d_bytes), "d2h_bytes": int(r.d2h_bytes), "live_states": int(r.live_states),
         "live_ms": float(r.live_ms), "live_rounds": int(r.live_rounds),
+        "table_generation": int(r.table_generation), "table_cleared": int(r.table_cleared),
         "expanded": int(r.expanded), "launches": int(r.launches), "explore_ms": float(r.explore_ms),
         "kernel_ms": float(r.kernel_ms), "setup_ms": float(r.setup_ms), "set_hash": f"{r.set_hash:016x}",
         "key_words": int(r.key_words), "table_count": int(r.table_count), "table_slots": int(r.table_slots),

@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define GPX_ABI_VERSION 2
+#define GPX_ABI_VERSION 3
 
 /* Status codes.  They replace the reference's exit(1) paths. */
 typedef enum {
@@ -110,6 +110,11 @@ typedef struct {
     uint64_t live_states;    /* liveness: states left in the accepting-cycle fixpoint (0 = no accepting cycle) */
     double live_ms;          /* liveness: device time of the accepting-cycle check */
     uint64_t live_rounds;    /* liveness: frontier rounds (forward closure and peeling) of the check */
+    uint32_t table_generation; /* 128-bit slots of a reusable explorer table (state vectors of 64..112
+                                  bits): the generation (1..255) this run's keys carry; slots of other
+                                  generations read as free, so only some runs clear the table; 0 for
+                                  the untagged slot forms, which every run clears */
+    int32_t table_cleared;   /* this run zeroed the hash table before it started */
 } gpx_result;
 
 typedef struct gpx_model gpx_model;

@@ -108,8 +108,10 @@ def test_high_load_bounded_eviction(gpu, tmp_path, slots_per_state):
 
 
 # exact key-width boundaries: 31/32 bits (32- vs 64-bit slots), 63/64 (64- vs
-# 128-bit), and 126 bits over 31 processes (the widest vector and the process limit)
-WIDTHS = {31: [15] * 7 + [7], 32: [15] * 8, 63: [15] * 15 + [7], 64: [15] * 16, 126: [31, 31] + [15] * 29}
+# 128-bit), 112/113 (generation-tagged vs untagged 128-bit slots), and 126 bits
+# over 31 processes (the widest vector and the process limit)
+WIDTHS = {31: [15] * 7 + [7], 32: [15] * 8, 63: [15] * 15 + [7], 64: [15] * 16, 112: [15] * 28,
+          113: [31] + [15] * 27, 126: [31, 31] + [15] * 29}
 
 
 @pytest.mark.parametrize("bits", sorted(WIDTHS))
@@ -123,3 +125,4 @@ def test_width_boundaries(gpu, tmp_path, bits, flags):
     g = _gpu(gpu, path, kw, max_states=60_000)
     _same(o, g)
     assert g["slot_bytes"] == (4 if bits <= 31 else (8 if bits <= 63 else 16))
+    assert g["table_generation"] == (1 if 64 <= bits <= 112 else 0)

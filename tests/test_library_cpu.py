@@ -62,7 +62,7 @@ def test_status_strings(built):
     from gpuexplore_gb300 import lib
     L = lib.load()
     assert L.gpx_status_string(4) == b"problem with hash table"
-    assert L.gpx_abi_version() == 2
+    assert L.gpx_abi_version() == 3
 
 
 def test_no_gpu_is_a_status(built, tmp_path):
