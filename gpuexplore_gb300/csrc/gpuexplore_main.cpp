@@ -40,6 +40,7 @@ static const char *kHelp =
     "  --por-model FILE   Use the learned cluster proposal in FILE (a gpx_por_model) with --por\n"
     "  --ample            Partial-order reduction with single-process ample sets\n"
     "  --stubborn         Partial-order reduction with stubborn sets (necessary enabling processes)\n"
+    "  --no-prune         Generate every successor in plain exploration (no commuting-move pruning)\n"
     "  -h, --help         Show this help message\n";
 
 static uint64_t mix64(uint64_t z) {
@@ -111,6 +112,9 @@ int main(int argc, char **argv) {
             i += 1;
         } else if (!strcmp(a, "--stubborn")) {
             o.por = 4; // stubborn sets from necessary enabling processes
+            i += 1;
+        } else if (!strcmp(a, "--no-prune")) {
+            o.prune_commuting = 0;
             i += 1;
         } else if (!strcmp(a, "--cycle-proviso")) {
             if (o.property == GPX_PROP_NONE) o.cycle_proviso = 1; // only before -d/-p

@@ -57,7 +57,7 @@ struct alignas(128) Ctrl {
     alignas(128) unsigned int bar_count;         // grid barrier arrivals
     alignas(128) unsigned int bar_gen;           // grid barrier generation (polled by waiting blocks)
     alignas(128) unsigned long long lookups; // statistics (one line)
-    unsigned long long probes, expanded, inserts, inserts_lookups;
+    unsigned long long probes, expanded, inserts, inserts_lookups, pruned;
 };
 
 struct Params {
@@ -90,6 +90,9 @@ struct Params {
     unsigned long long log_cap;
     // the run's key generation, written by the host before the run (null: 0)
     const unsigned long long *gen;
+    // plain mode: per store position, the participants of the move that first
+    // inserted the state (0: none); null disables commuting-move pruning
+    uint32_t *label;
 };
 
 // ------------------------------------------------------------- device helpers
@@ -405,9 +408,9 @@ __device__ int place_evicting(K *table, unsigned long long nb, const K &key, uns
 // Place the level's overflowed keys (single thread, table quiescent); new ones
 // are appended to the store.  Sets GPX_ERR_TABLE_FULL when one cannot be placed.
 template <class K>
-__device__ void place_overflow(K *table, unsigned long long nb, K *store, unsigned long long store_cap,
-                               const K *overflow, unsigned long long overflow_cap, Ctrl *c,
-                               unsigned long long seed) {
+__device__ void place_overflow(K *table, unsigned long long nb, K *store, uint32_t *label,
+                               unsigned long long store_cap, const K *overflow, unsigned long long overflow_cap,
+                               Ctrl *c, unsigned long long seed) {
     unsigned long long n = c->overflow_count;
     if (n > overflow_cap) {
         n = overflow_cap;
@@ -423,10 +426,12 @@ __device__ void place_overflow(K *table, unsigned long long nb, K *store, unsign
         }
         if (r == 1) {
             unsigned long long idx = c->store_count++;
-            if (idx < store_cap)
+            if (idx < store_cap) {
                 store[idx] = key;
-            else
+                if (label) label[idx] = 0; // its inserting move is not kept: nothing is pruned from it
+            } else {
                 atomicCAS(&c->error, 0u, (unsigned int)GPX_ERR_STORE_FULL);
+            }
             c->inserts++;
         }
     }
@@ -474,13 +479,18 @@ template <class K, int MODE> struct WarpScratch {
     uint32_t clo[kPor];          // per pair: cluster closure
     uint32_t nw[kPor];           // per pair: successors not yet visited (decide pass, for the log)
     uint16_t cand[kPor];         // learned proposal / log: the pairs whose closure is scored
-    uint32_t prov[32], sel[32], best[32], vmask[32];
-    unsigned long long lbest[32]; // learned proposal: (sortable score, popcount, process)
+    static constexpr int kSrc = (MODE == MODE_PLAIN) ? 1 : 32; // per-state arrays of the POR modes
+    static constexpr int kLab = (MODE == MODE_PLAIN) ? 32 : 1; // ... and of plain mode
+    uint32_t prov[32], sel[32], best[kSrc], vmask[kSrc];
+    unsigned long long lbest[kSrc]; // learned proposal: (sortable score, popcount, process)
+    uint32_t lab[kLab];                        // label of each source state
+    uint32_t slab[kLab == 1 ? 1 : kStage];     // labels of the staged new states
 };
 
 struct WarpStats {
     unsigned int lookups, probes, inserts, expanded, ilookups;
     unsigned int violation;
+    unsigned int pruned;
 };
 
 // Model accessors over the device layout (gpx_model.h).  The array bases are
@@ -619,7 +629,7 @@ template <class K, int MODE> struct Explorer {
         lane = threadIdx.x & 31;
         lanemask_lt = (1u << lane) - 1u;
         shead = scount = 0;
-        st = WarpStats{0, 0, 0, 0, 0, 0};
+        st = WarpStats{0, 0, 0, 0, 0, 0, 0};
         safety = P.property == GPX_PROP_SAFETY;
         deadlock = P.property == GPX_PROP_DEADLOCK;
     }
@@ -643,9 +653,10 @@ template <class K, int MODE> struct Explorer {
         base = __shfl_sync(kFull, base, 0);
         if (lane < cnt) {
             unsigned long long idx = base + lane;
-            if (idx < P.store_cap)
+            if (idx < P.store_cap) {
                 store[idx] = ws.stage[(shead + lane) % kStage];
-            else
+                if (MODE == MODE_PLAIN && P.label) P.label[idx] = ws.slab[(shead + lane) % kStage];
+            } else
                 set_error(P.ctrl, GPX_ERR_STORE_FULL);
         }
         shead = (shead + cnt) % kStage;
@@ -670,7 +681,8 @@ template <class K, int MODE> struct Explorer {
         K key = ws.keys[og];
         const uint32_t dp = M.pd(p);
         const uint32_t *rec = M.rec_of(dp, KT<K>::get(key, MView::fb_of(dp), MView::bs_of(dp)));
-        uint32_t lcnt = (!filter || (ws.sel[og] >> p & 1u)) ? rec[R_LCNT] : 0u;
+        // plain mode: sel holds the processes whose local moves are not pruned
+        uint32_t lcnt = ((MODE != MODE_PLAIN && !filter) || (ws.sel[og] >> p & 1u)) ? rec[R_LCNT] : 0u;
         out = key;
         omask = 0;
         if (sub < lcnt) {
@@ -711,11 +723,17 @@ template <class K, int MODE> struct Explorer {
             ws.keys[lane] = KT<K>::load(store + first + lane);
             ws.en[lane] = 0;
             ws.prov[lane] = 0;
-            ws.best[lane] = kFull;
             ws.sel[lane] = kFull;
             if (MODE != MODE_PLAIN) {
+                ws.best[lane] = kFull;
                 ws.vmask[lane] = 0;
                 ws.lbest[lane] = ~0ull;
+            } else {
+                // commuting-move pruning: local moves of processes below the
+                // label's lowest participant are generated from another state
+                const uint32_t lab = P.label ? __ldcg(P.label + first + lane) : 0u;
+                ws.lab[lane] = lab;
+                if (lab) ws.sel[lane] = ~((1u << (__ffs(lab) - 1)) - 1u);
             }
         }
         __syncwarp();
@@ -731,7 +749,16 @@ template <class K, int MODE> struct Explorer {
             uint32_t s;
             const uint32_t *rec = M.state_rec(key, p, s);
             uint32_t lcnt = rec[R_LCNT], roff = rec[R_ROFF], rcnt = rec[R_RCNT];
-            uint32_t appl = 0, provbits = lcnt ? (1u << p) : 0u, cnt = lcnt;
+            // Commuting-move pruning (plain mode).  The source was first inserted
+            // by a move with participants `lab`.  A move led by a process below
+            // lab's lowest participant and disjoint from lab commutes with it:
+            // its successor also follows from the other order, through a state
+            // of this same level with a higher-led move, so it is not generated
+            // here.  Enabledness and the safety check see every move.
+            const uint32_t lab = (MODE == MODE_PLAIN) ? ws.lab[g] : 0u;
+            const bool below = lab && p < (uint32_t)(__ffs(lab) - 1);
+            uint32_t appl = 0, keep = 0, provbits = lcnt ? (1u << p) : 0u, cnt = below ? 0u : lcnt;
+            uint32_t pruned = below ? lcnt : 0u;
             bool viol = safety && check && p == n - 1 && (rec[R_FLAGS] & 1u);
             for (uint32_t r = 0; r < rcnt; r++) {
                 uint32_t k = M.lrule(roff + r);
@@ -753,12 +780,18 @@ template <class K, int MODE> struct Explorer {
                 if (ok) {
                     appl |= 1u << r;
                     provbits |= mask;
-                    cnt += psz;
+                    if (below && (mask & lab) == 0) {
+                        pruned += psz;
+                    } else {
+                        keep |= 1u << r;
+                        cnt += psz;
+                    }
                     if (safety && check && hit1) viol = true;
                 }
             }
-            ws.appl[i] = appl;
+            ws.appl[i] = keep;
             ws.pre[i] = cnt;
+            st.pruned += pruned;
             if (MODE != MODE_PLAIN) {
                 // clusters feed the selection: the single POR pass, or the decide pass
                 if (MODE == MODE_POR || decide)
@@ -855,7 +888,9 @@ template <class K, int MODE> struct Explorer {
             uint32_t ins = __ballot_sync(kFull, res == 1);
             if (ins) {
                 if (res == 1) {
-                    ws.stage[(shead + scount + __popc(ins & lanemask_lt)) % kStage] = out;
+                    const uint32_t pos = (shead + scount + __popc(ins & lanemask_lt)) % kStage;
+                    ws.stage[pos] = out;
+                    if (MODE == MODE_PLAIN) ws.slab[pos] = omask;
                     st.inserts++;
                 }
                 scount += __popc(ins);
@@ -1064,14 +1099,15 @@ template <class K, int MODE> struct Explorer {
         if (scount) stage_flush(scount);
         if (__any_sync(kFull, st.violation) && lane == 0) atomicOr(&P.ctrl->violation, 1u);
         st.violation = 0;
-        if (__any_sync(kFull, st.probes > (1u << 30) || st.lookups > (1u << 30))) flush_counters();
+        if (__any_sync(kFull, st.probes > (1u << 30) || st.lookups > (1u << 30) || st.pruned > (1u << 30)))
+            flush_counters();
     }
 
     __device__ void flush_counters() {
         Ctrl *c = P.ctrl;
-        unsigned long long v[5] = {st.lookups, st.probes, st.inserts, st.expanded, st.ilookups};
+        unsigned long long v[6] = {st.lookups, st.probes, st.inserts, st.expanded, st.ilookups, st.pruned};
 #pragma unroll
-        for (int k = 0; k < 5; k++)
+        for (int k = 0; k < 6; k++)
             for (int o = 16; o; o >>= 1) v[k] += __shfl_xor_sync(kFull, v[k], o);
         if (lane == 0) {
             if (v[0]) atomicAdd(&c->lookups, v[0]);
@@ -1079,8 +1115,9 @@ template <class K, int MODE> struct Explorer {
             if (v[2]) atomicAdd(&c->inserts, v[2]);
             if (v[3]) atomicAdd(&c->expanded, v[3]);
             if (v[4]) atomicAdd(&c->inserts_lookups, v[4]);
+            if (v[5]) atomicAdd(&c->pruned, v[5]);
         }
-        st = WarpStats{0, 0, 0, 0, 0, st.violation};
+        st = WarpStats{0, 0, 0, 0, 0, st.violation, 0};
     }
 
     __device__ void flush_stats() {

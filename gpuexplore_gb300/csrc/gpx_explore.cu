@@ -64,8 +64,8 @@ template <class K, int MODE> __device__ void close_phase(const Params &P) {
         return;
     }
     if (c->overflow_count)
-        place_overflow<K>((K *)P.table, P.nbuckets, (K *)P.store, P.store_cap, (const K *)P.overflow, P.overflow_cap,
-                          c, P.seed);
+        place_overflow<K>((K *)P.table, P.nbuckets, (K *)P.store, P.label, P.store_cap, (const K *)P.overflow,
+                          P.overflow_cap, c, P.seed);
     unsigned long long hi = c->hi;
     unsigned long long newhi = c->store_count;
     if (newhi > P.store_cap) newhi = P.store_cap;
@@ -221,6 +221,7 @@ template <class K> __global__ void init_kernel(Params P, unsigned int first_phas
     unsigned int probes = 0;
     find_or_insert<K>((K *)P.table, P.nbuckets, key, KT<K>::hash(key, P.seed), probes);
     ((K *)P.store)[0] = key;
+    if (P.label) P.label[0] = 0;
     P.levels[0] = 1;
 }
 
@@ -397,6 +398,7 @@ struct gpx_explorer {
     uint32_t *d_model = nullptr;
     size_t model_cap_words = 0;
     uint32_t *d_sel = nullptr;
+    uint32_t *d_label = nullptr; // plain mode with prune_commuting: inserting move per store position
     void *d_overflow = nullptr; // keys whose probe sequence was full during a level
     unsigned long long overflow_cap = 0;
     unsigned long long *d_levels = nullptr;
@@ -517,6 +519,7 @@ Params make_params(gpx_explorer *ex) {
     P.model_words = (uint32_t)ex->model.dec.words.size();
     P.model_in_smem = ex->model_in_smem;
     P.sel = ex->d_sel;
+    P.label = ex->mode == MODE_PLAIN ? ex->d_label : nullptr;
     P.overflow = ex->d_overflow;
     P.overflow_cap = ex->overflow_cap;
     P.levels = ex->d_levels;
@@ -749,6 +752,7 @@ void gpx_options_init(gpx_options *o) {
     o->struct_size = sizeof *o;
     o->seed = 0x243F6A8885A308D3ull;
     o->launch_graph = 1;
+    o->prune_commuting = 1;
 }
 
 int gpx_model_load(const char *path_without_ext, gpx_model **out) {
@@ -812,6 +816,7 @@ void gpx_explorer_destroy(gpx_explorer *ex) {
     if (ex->d_store) cudaFree(ex->d_store);
     if (ex->d_model) cudaFree(ex->d_model);
     if (ex->d_sel) cudaFree(ex->d_sel);
+    if (ex->d_label) cudaFree(ex->d_label);
     if (ex->d_overflow) cudaFree(ex->d_overflow);
     if (ex->d_levels) cudaFree(ex->d_levels);
     if (ex->d_scalar) cudaFree(ex->d_scalar);
@@ -868,7 +873,8 @@ int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_exp
     ex->table_bytes = tb;
     ex->nbuckets = tb / bucket_bytes;
     ex->slots = ex->nbuckets * ex->ks.bucket_slots;
-    const size_t per_state = ex->ks.slot_bytes + (ex->mode == MODE_PROVISO ? 4 : 0);
+    const bool labels = ex->mode == MODE_PLAIN && opts->prune_commuting;
+    const size_t per_state = ex->ks.slot_bytes + (ex->mode == MODE_PROVISO || labels ? 4 : 0);
     unsigned long long cap = opts->store_states ? opts->store_states : ex->slots;
     size_t margin = (size_t)512 << 20;
     size_t avail = free_b > tb + margin ? free_b - tb - margin : 0;
@@ -878,6 +884,7 @@ int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_exp
     if (cudaMalloc(&ex->d_table, tb) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (cudaMalloc(&ex->d_store, cap * ex->ks.slot_bytes) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (ex->mode == MODE_PROVISO && cudaMalloc(&ex->d_sel, cap * 4) != cudaSuccess) return fail(GPX_ERR_NOMEM);
+    if (labels && cudaMalloc(&ex->d_label, cap * 4) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     ex->overflow_cap = 1u << 16;
     if (cudaMalloc(&ex->d_overflow, ex->overflow_cap * ex->ks.slot_bytes) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (cudaMalloc(&ex->d_levels, (size_t)kMaxLevels * 8) != cudaSuccess) return fail(GPX_ERR_NOMEM);
@@ -1012,6 +1019,7 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     r->probes = c.probes;
     r->inserts = c.inserts;
     r->evictions = c.evictions;
+    r->pruned = c.pruned;
     r->expanded = c.expanded;
     r->launches = launches;
     r->kernel_ms = kernel_ms;

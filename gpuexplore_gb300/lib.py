@@ -72,7 +72,7 @@ class Options(C.Structure):
         ("por", C.c_int32), ("cycle_proviso", C.c_int32), ("property", C.c_int32), ("device", C.c_int32),
         ("seed", C.c_uint64), ("max_states", C.c_uint64), ("store_states", C.c_uint64),
         ("collect_states", C.c_int32), ("bucket_bytes", C.c_int32),
-        ("launch_graph", C.c_int32),
+        ("launch_graph", C.c_int32), ("prune_commuting", C.c_int32),
     ]
 
 
@@ -88,6 +88,7 @@ class Result(C.Structure):
         ("inserts", C.c_uint64), ("evictions", C.c_uint64),
         ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("live_states", C.c_uint64), ("live_ms", C.c_double),
         ("live_rounds", C.c_uint64), ("table_generation", C.c_uint32), ("table_cleared", C.c_int32),
+        ("pruned", C.c_uint64),
     ]
 
 
@@ -273,6 +274,7 @@ def _result_dict(r: Result) -> Dict:
         "h2d_bytes": int(r.h2d_bytes), "d2h_bytes": int(r.d2h_bytes), "live_states": int(r.live_states),
         "live_ms": float(r.live_ms), "live_rounds": int(r.live_rounds),
         "table_generation": int(r.table_generation), "table_cleared": int(r.table_cleared),
+        "pruned": int(r.pruned),
         "expanded": int(r.expanded), "launches": int(r.launches), "explore_ms": float(r.explore_ms),
         "kernel_ms": float(r.kernel_ms), "setup_ms": float(r.setup_ms), "set_hash": f"{r.set_hash:016x}",
         "key_words": int(r.key_words), "table_count": int(r.table_count), "table_slots": int(r.table_slots),

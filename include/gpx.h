@@ -76,6 +76,11 @@ typedef struct {
     int32_t launch_graph;   /* 1 (gpx_options_init): with verbosity 0, a run is one CUDA graph -- reset, init,
                                a device-side loop over the exploration launches (the -k relaunch loop),
                                set hash and read-back -- built once and replayed; 0: host-driven launches */
+    int32_t prune_commuting; /* 1 (gpx_options_init), plain exploration by a gpx_explorer: a state does not
+                                generate the successors of moves that commute with the move that first
+                                inserted it and are led by a lower process -- a state of the same level
+                                generates each of them -- so fewer lookups reach the table; the visited
+                                set, level counts and verdicts are unchanged; 0: every successor */
 } gpx_options;
 
 /* Result of one exploration.  Arrays are owned by the library: gpx_result_free. */
@@ -115,6 +120,9 @@ typedef struct {
                                   generations read as free, so only some runs clear the table; 0 for
                                   the untagged slot forms, which every run clears */
     int32_t table_cleared;   /* this run zeroed the hash table before it started */
+    uint64_t pruned;         /* successors not generated by commuting-move pruning (gpx_options.prune_commuting);
+                                with it, lookups/transitions/probes depend on which of a state's predecessors
+                                inserted it first and vary between runs */
 } gpx_result;
 
 typedef struct gpx_model gpx_model;

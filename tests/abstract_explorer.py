@@ -147,6 +147,45 @@ def explore(net: Network, prop: str = "none", por: bool = False, proviso: bool =
             "visited": visited}
 
 
+def explore_pruned(net: Network, rng, max_states: int = 0) -> Dict:
+    """Plain BFS with commuting-move pruning, restated independently of the
+    kernel: every new state is labelled with the participants of the move that
+    first inserted it; a state does not generate a move led by a process below
+    its label's lowest participant that is disjoint from the label.  Expansion
+    and successor order are shuffled with `rng`, so the labels -- which
+    predecessor inserts a state first -- vary as they do between GPU runs."""
+    n = net.nprocs
+    init: State = tuple([0] * n)
+    label: Dict[State, int] = {init: 0}
+    frontier = [init]
+    levels = [1]
+    generated = pruned = 0
+    while frontier:
+        rng.shuffle(frontier)
+        nxt: List[State] = []
+        for s in frontier:
+            lab = label[s]
+            low = (lab & -lab).bit_length() - 1
+            succ = successors(net, s)
+            rng.shuffle(succ)
+            for t, mask in succ:
+                lead = (mask & -mask).bit_length() - 1
+                if lab and lead < low and mask & lab == 0:
+                    pruned += 1
+                    continue
+                generated += 1
+                if t not in label:
+                    label[t] = mask
+                    nxt.append(t)
+        if nxt:
+            levels.append(len(nxt))
+        frontier = nxt
+        if max_states and len(label) >= max_states and frontier:
+            break
+    return {"states": len(label), "levels": levels, "visited": set(label), "generated": generated,
+            "pruned": pruned}
+
+
 def pack(net: Network, s: State) -> List[int]:
     """Pack a state tuple into gpf state-vector words (firstbit layout)."""
     fb = net.firstbit()

@@ -81,7 +81,8 @@ def test_cli_surface(built, tmp_path):
     assert r.returncode == 1 and "No input network given" in r.stderr
     r = subprocess.run([cli, "--help"], capture_output=True, text=True)
     assert r.returncode == 0 and "Usage: gpuexplore" in r.stdout
-    for flag in ("--por", "--cycle-proviso", "--ample", "--stubborn", "--por-model", "--dump", "-k", "-q"):
+    for flag in ("--por", "--cycle-proviso", "--ample", "--stubborn", "--por-model", "--dump", "-k", "-q",
+                 "--no-prune"):
         assert flag in r.stdout, flag
     r = subprocess.run([cli, str(tmp_path / "x"), "-z"], capture_output=True, text=True)
     assert r.returncode == 1 and "unrecognized option -z" in r.stderr
@@ -107,6 +108,7 @@ def test_option_defaults(built):
     from gpuexplore_gb300 import lib
     o = lib.options()
     assert o.launch_graph == 1 and o.por == 0 and o.kernel_iters == 0 and o.bucket_bytes == 0
+    assert o.prune_commuting == 1
     L = lib.load()
     b = lib.BatchOptions()
     L.gpx_batch_options_init(lib.C.byref(b))

@@ -26,7 +26,7 @@ def test_noalloc_matches_explore(gpu, case):
     else:
         net, kw = gen.random_network(13, nprocs=24, states=(4, 9), outdeg=(1, 2)), dict(max_states=300_000)
     m = _model(lib, net)
-    ref = lib.explore(m, q_words=1 << 22, **kw)
+    ref = lib.explore(m, q_words=1 << 22, prune_commuting=0, **kw)  # the no-allocation path does not prune
     # two calls in a row: the second reuses the array the first left behind
     for _ in range(2):
         got = lib.explore_noalloc(m, **kw)
