@@ -174,7 +174,8 @@ static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char 
     if (B > claim) B = (uint32_t)claim; // small claims: one batch per claim, spread over warps
     for (unsigned long long b = off; b < off + cnt; b += B) {
         uint32_t n = (uint32_t)((off + cnt - b) < B ? (off + cnt - b) : B);
-        E.batch(lo + b, n, b, decide);
+        unsigned long long left = off + cnt - b - n;
+        E.batch(lo + b, n, b, decide, (uint32_t)(left < B ? left : B));
     }
     E.flush_stats(); // appends the staged new states before the chunk is reported
 }

@@ -110,6 +110,10 @@ static __device__ __forceinline__ uint64_t globaltimer() {
     return t;
 }
 
+static __device__ __forceinline__ void prefetch_l2(const void *p) {
+    asm volatile("prefetch.global.L2 [%0];" : : "l"(p));
+}
+
 static __device__ __forceinline__ void ld256_cg(const void *p, uint32_t (&w)[8]) {
     asm volatile("ld.global.cg.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
@@ -466,6 +470,7 @@ __device__ __forceinline__ bool find_key(K *table, unsigned long long nb, const 
 // --------------------------------------------------------- per-warp scratch
 
 constexpr int kStage = 64; // new states staged per warp before one store append
+constexpr uint32_t kRuleQueue = 64; // (pair, rule) items queued per warp in phase A
 
 template <class K, int MODE> struct WarpScratch {
     static constexpr int kPairs = (MODE == MODE_PLAIN) ? kPairMax : kPairMaxPor;
@@ -481,10 +486,11 @@ template <class K, int MODE> struct WarpScratch {
     uint16_t cand[kPor];         // learned proposal / log: the pairs whose closure is scored
     static constexpr int kSrc = (MODE == MODE_PLAIN) ? 1 : 32; // per-state arrays of the POR modes
     static constexpr int kLab = (MODE == MODE_PLAIN) ? 32 : 1; // ... and of plain mode
-    uint32_t prov[32], sel[32], best[kSrc], vmask[kSrc];
+    uint32_t prov[kSrc], sel[32], best[kSrc], vmask[kSrc];
     unsigned long long lbest[kSrc]; // learned proposal: (sortable score, popcount, process)
     uint32_t lab[kLab];                        // label of each source state
     uint32_t slab[kLab == 1 ? 1 : kStage];     // labels of the staged new states
+    uint16_t ritem[kRuleQueue];                // queued (pair << 5 | rule) items of phase A
 };
 
 struct WarpStats {
@@ -716,15 +722,63 @@ template <class K, int MODE> struct Explorer {
         }
     }
 
-    // Expand a batch of B states store[first .. first+B).
-    __device__ void batch(unsigned long long first, uint32_t B, unsigned long long lvl_off, bool decide) {
+    // Plain mode: is pair (g, p) below the lowest participant of the move that
+    // first inserted state g (its local moves, and its rules disjoint from that
+    // move, are pruned)?
+    __device__ bool pruned_below(uint32_t g, uint32_t p) const {
+        if (MODE != MODE_PLAIN) return false;
+        const uint32_t lab = ws.lab[g];
+        return lab && p < (uint32_t)(__ffs(lab) - 1);
+    }
+
+    // Rule number r among those pair i leads: applicable when every member has
+    // its action enabled; its successors (the product of the members' targets)
+    // are added to the pair's count unless pruned.
+    __device__ void eval_rule(uint32_t i, uint32_t r, bool check) {
         const uint32_t n = M.n;
+        const uint32_t g = i / n, p = i - g * n;
+        const K key = ws.keys[g];
+        uint32_t s;
+        const uint32_t *rec = M.state_rec(key, p, s);
+        const uint32_t k = M.lrule(rec[R_ROFF] + r);
+        const uint32_t mask = M.rmask(k), act = M.ract(k);
+        bool hit1 = false;
+        uint32_t rest = mask, psz = 1;
+        while (rest) {
+            const uint32_t q = __ffs(rest) - 1;
+            rest &= rest - 1;
+            uint32_t sq;
+            const uint32_t *grp = M.group(q == p ? rec : M.state_rec(key, q, sq), act);
+            if (!grp) return;
+            psz *= grp[2];
+            if (q == n - 1 && (grp[3] & 1u)) hit1 = true;
+        }
+        ws.en[g] = 1;
+        if (MODE == MODE_POR) atomicOr(&ws.prov[g], mask);
+        if (pruned_below(g, p) && (mask & ws.lab[g]) == 0) {
+            st.pruned += psz;
+        } else {
+            atomicOr(&ws.appl[i], 1u << r);
+            atomicAdd(&ws.pre[i], psz);
+        }
+        if (safety && check && hit1) st.violation = 1;
+    }
+
+    // Expand a batch of B states store[first .. first+B); the next `ahead`
+    // states of the warp's claim are fetched into L2 meanwhile.
+    __device__ void batch(unsigned long long first, uint32_t B, unsigned long long lvl_off, bool decide,
+                          uint32_t ahead) {
+        const uint32_t n = M.n;
+        if (lane < ahead) {
+            prefetch_l2(store + first + B + lane);
+            if (MODE == MODE_PLAIN && P.label) prefetch_l2(P.label + first + B + lane);
+        }
         if (lane < B) {
             ws.keys[lane] = KT<K>::load(store + first + lane);
             ws.en[lane] = 0;
-            ws.prov[lane] = 0;
             ws.sel[lane] = kFull;
             if (MODE != MODE_PLAIN) {
+                ws.prov[lane] = 0;
                 ws.best[lane] = kFull;
                 ws.vmask[lane] = 0;
                 ws.lbest[lane] = ~0ull;
@@ -742,65 +796,74 @@ template <class K, int MODE> struct Explorer {
         const bool filter = (MODE == MODE_POR) || (MODE == MODE_PROVISO && !decide);
 
         // A: enabledness, applicable rules, successor counts, static clusters,
-        //    safety on moves into monitor state 1 (GPUexplore.cu:927-935, 1063-1069)
-        for (uint32_t i = lane; i < npairs; i += 32) {
-            uint32_t g = i / n, p = i - g * n;
-            K key = ws.keys[g];
-            uint32_t s;
-            const uint32_t *rec = M.state_rec(key, p, s);
-            uint32_t lcnt = rec[R_LCNT], roff = rec[R_ROFF], rcnt = rec[R_RCNT];
-            // Commuting-move pruning (plain mode).  The source was first inserted
-            // by a move with participants `lab`.  A move led by a process below
-            // lab's lowest participant and disjoint from lab commutes with it:
-            // its successor also follows from the other order, through a state
-            // of this same level with a higher-led move, so it is not generated
-            // here.  Enabledness and the safety check see every move.
-            const uint32_t lab = (MODE == MODE_PLAIN) ? ws.lab[g] : 0u;
-            const bool below = lab && p < (uint32_t)(__ffs(lab) - 1);
-            uint32_t appl = 0, keep = 0, provbits = lcnt ? (1u << p) : 0u, cnt = below ? 0u : lcnt;
-            uint32_t pruned = below ? lcnt : 0u;
-            bool viol = safety && check && p == n - 1 && (rec[R_FLAGS] & 1u);
-            for (uint32_t r = 0; r < rcnt; r++) {
-                uint32_t k = M.lrule(roff + r);
-                uint32_t mask = M.rmask(k), act = M.ract(k);
-                bool ok = true, hit1 = false;
-                uint32_t rest = mask, psz = 1;
-                while (rest) {
-                    uint32_t q = __ffs(rest) - 1;
-                    rest &= rest - 1;
-                    uint32_t sq;
-                    const uint32_t *grp = M.group(q == p ? rec : M.state_rec(key, q, sq), act);
-                    if (!grp) {
-                        ok = false;
-                        break;
-                    }
-                    psz *= grp[2];
-                    if (q == n - 1 && (grp[3] & 1u)) hit1 = true;
+        //    safety on moves into monitor state 1 (GPUexplore.cu:927-935, 1063-1069).
+        //    Local moves per (state, process) pair; the rules a pair leads are
+        //    queued as (pair, rule) items and evaluated 32 at a time, one per
+        //    lane, instead of by the few lanes whose pair has rules.
+        uint32_t rhead = 0, rcount = 0; // rule-item queue (warp-uniform)
+        for (uint32_t base = 0; base < npairs; base += 32) {
+            const uint32_t i = base + lane;
+            uint32_t rcnt = 0;
+            if (i < npairs) {
+                uint32_t g = i / n, p = i - g * n;
+                K key = ws.keys[g];
+                uint32_t s;
+                const uint32_t *rec = M.state_rec(key, p, s);
+                const uint32_t lcnt = rec[R_LCNT];
+                rcnt = rec[R_RCNT];
+                // Commuting-move pruning (plain mode).  The source was first
+                // inserted by a move with participants `lab`.  A move led by a
+                // process below lab's lowest participant and disjoint from lab
+                // commutes with it: its successor also follows from the other
+                // order, through a state of this same level with a higher-led
+                // move, so it is not generated here.  Enabledness and the safety
+                // check see every move.
+                const bool below = pruned_below(g, p);
+                ws.appl[i] = 0;
+                ws.pre[i] = below ? 0u : lcnt;
+                if (below) st.pruned += lcnt;
+                if (MODE != MODE_PLAIN) {
+                    // clusters feed the selection: the single POR pass, or the decide pass
+                    if (MODE == MODE_POR || decide)
+                        ws.cl0[i] = P.por_kind == POR_STUBBORN ? stubborn_cluster(key, p, rec) : rec[R_CL0];
+                    ws.nw[i] = 0;
                 }
-                if (ok) {
-                    appl |= 1u << r;
-                    provbits |= mask;
-                    if (below && (mask & lab) == 0) {
-                        pruned += psz;
-                    } else {
-                        keep |= 1u << r;
-                        cnt += psz;
-                    }
-                    if (safety && check && hit1) viol = true;
+                if (lcnt) {
+                    ws.en[g] = 1;
+                    if (MODE == MODE_POR) atomicOr(&ws.prov[g], 1u << p);
                 }
+                if (safety && check && p == n - 1 && (rec[R_FLAGS] & 1u)) st.violation = 1;
             }
-            ws.appl[i] = keep;
-            ws.pre[i] = cnt;
-            st.pruned += pruned;
-            if (MODE != MODE_PLAIN) {
-                // clusters feed the selection: the single POR pass, or the decide pass
-                if (MODE == MODE_POR || decide)
-                    ws.cl0[i] = P.por_kind == POR_STUBBORN ? stubborn_cluster(key, p, rec) : rec[R_CL0];
-                ws.nw[i] = 0;
+            uint32_t incl = rcnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(kFull, incl, o);
+                if (lane >= (uint32_t)o) incl += y;
             }
-            if (lcnt | appl) ws.en[g] = 1;
-            if (MODE == MODE_POR) atomicOr(&ws.prov[g], provbits);
-            if (viol) st.violation = 1;
+            const uint32_t T = __shfl_sync(kFull, incl, 31);
+            if (!T) continue;
+            if (rcount + T <= kRuleQueue) {
+                for (uint32_t x = 0, at = rhead + rcount + incl - rcnt; x < rcnt; x++)
+                    ws.ritem[(at + x) % kRuleQueue] = (uint16_t)((i << 5) | x);
+                rcount += T;
+                while (rcount >= 32) {
+                    __syncwarp();
+                    const uint32_t it = ws.ritem[(rhead + lane) % kRuleQueue];
+                    __syncwarp();
+                    eval_rule(it >> 5, it & 31u, check);
+                    rhead = (rhead + 32) % kRuleQueue;
+                    rcount -= 32;
+                }
+            } else {
+                // more items than the queue holds: this chunk's lanes evaluate their own
+                for (uint32_t x = 0; x < rcnt; x++) eval_rule(i, x, check);
+            }
+        }
+        if (rcount) {
+            __syncwarp();
+            const uint32_t it = ws.ritem[(rhead + lane) % kRuleQueue];
+            __syncwarp();
+            if (lane < rcount) eval_rule(it >> 5, it & 31u, check);
         }
         __syncwarp();
         if (deadlock && check && lane < B && ws.en[lane] == 0) st.violation = 1;

@@ -179,7 +179,8 @@ template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_k
             unsigned long long end = base + size < nlev ? base + size : nlev;
             for (unsigned long long b = base; b < end; b += B) {
                 uint32_t cnt = (uint32_t)((end - b) < B ? (end - b) : B);
-                E.batch(lo + b, cnt, b, decide);
+                unsigned long long left = end - b - cnt;
+                E.batch(lo + b, cnt, b, decide, (uint32_t)(left < B ? left : B));
             }
             if (static_end >= nlev) break;
             base = nlev;
