@@ -190,11 +190,14 @@ template <> struct KT<K64> {
 // Shared by the two 128-bit slot forms: the state vector is split into a low
 // part of S bits (in the low 64-bit half) and the rest (in the high half).
 template <uint32_t S> struct Split128 {
+    // Without branches (the lanes of a warp read fields of different halves):
+    // the state vector as one 2S-bit value x1:x0, then a funnel shift.
     __device__ static uint32_t get(unsigned long long lo, unsigned long long hi, uint32_t f, uint32_t w) {
-        if (f + w <= S) return (uint32_t)((lo >> f) & lmask(w));
-        if (f >= S) return (uint32_t)((hi >> (f - S)) & lmask(w));
-        uint32_t nlo = S - f;
-        return (uint32_t)(((lo >> f) & lmask(nlo)) | ((hi & lmask(w - nlo)) << nlo));
+        constexpr unsigned long long m = (1ull << S) - 1ull;
+        const unsigned long long h = hi & m;
+        const unsigned long long x0 = (lo & m) | (h << S), x1 = h >> (64 - S);
+        const unsigned long long v = f >= 64 ? (x1 >> (f - 64)) : ((x0 >> f) | ((x1 << 1) << (63 - f)));
+        return (uint32_t)(v & lmask(w));
     }
     __device__ static void set(unsigned long long &lo, unsigned long long &hi, uint32_t f, uint32_t w, uint32_t x) {
         if (f + w <= S) {
@@ -801,11 +804,12 @@ template <class K, int MODE> struct Explorer {
         //    queued as (pair, rule) items and evaluated 32 at a time, one per
         //    lane, instead of by the few lanes whose pair has rules.
         uint32_t rhead = 0, rcount = 0; // rule-item queue (warp-uniform)
+        const uint32_t q32 = 32u / n, r32 = 32u - q32 * n;
+        uint32_t g = lane / n, p = lane - g * n; // pair i = g * n + p, stepped by 32
         for (uint32_t base = 0; base < npairs; base += 32) {
             const uint32_t i = base + lane;
             uint32_t rcnt = 0;
             if (i < npairs) {
-                uint32_t g = i / n, p = i - g * n;
                 K key = ws.keys[g];
                 uint32_t s;
                 const uint32_t *rec = M.state_rec(key, p, s);
@@ -833,6 +837,12 @@ template <class K, int MODE> struct Explorer {
                     if (MODE == MODE_POR) atomicOr(&ws.prov[g], 1u << p);
                 }
                 if (safety && check && p == n - 1 && (rec[R_FLAGS] & 1u)) st.violation = 1;
+            }
+            g += q32;
+            p += r32;
+            if (p >= n) {
+                p -= n;
+                g++;
             }
             uint32_t incl = rcnt;
 #pragma unroll
