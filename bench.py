@@ -440,7 +440,7 @@ def main():
     # clear is charged to every step, amortised over the runs it serves.
     cleared = [x["setup_ms"] for x in warm + results if x["table_cleared"]]
     plain = [x["setup_ms"] for x in warm + results if not x["table_cleared"]]
-    clear_ms = (max(cleared) - (min(plain) if plain else 0.0)) if cleared else 0.0
+    clear_ms = max(0.0, max(cleared) - (min(plain) if plain else 0.0)) if cleared else 0.0
     per_clear = 255 if r["table_generation"] else 1
     amortised = clear_ms / per_clear if any(not x["table_cleared"] for x in results) else 0.0
     step_ms, e2e_step = max_over_ranks(sum(dev_ms) / len(dev_ms) + amortised,
@@ -460,8 +460,13 @@ def main():
             pj = json.load(f)
         if pj.get("states") == r["states"] and pj.get("kernel_build") == KERNEL_BUILD:
             traffic = pj["dram_bytes_read"] + pj["dram_bytes_write"]
-    # the random-access ceiling: 32-byte sectors gathered at random over 20 GB
+    # the random-access ceilings over 20 GB: 32-byte sectors gathered at random,
+    # and insert-like accesses (read a random bucket, CAS a slot of it: the
+    # sector is dirtied and written back).  Every insert is one of the latter,
+    # the other bucket probes are gathers: their sum is the table's time floor.
     gathers = lib.random_gather_rate(local, 20 << 30)
+    rmw = lib.random_insert_rate(local, 20 << 30)
+    floor_ms = (r["inserts"] / rmw + max(0, r["probes"] - r["inserts"]) / gathers) * 1000.0
     line = {
         "metric": "new states/s", "value": value, "unit": "states/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -483,10 +488,11 @@ def main():
                      "lookups": r["lookups"], "inserts": r["inserts"], "expanded": r["expanded"],
                      "probes": r["probes"],
                      "random_access": {"probes_per_s": r["probes"] / (kms / 1000.0),
-                                       "peak_gathers_per_s": gathers,
-                                       "frac": r["probes"] / (kms / 1000.0) / gathers,
-                                       "how": "gpx_random_gather_probe: random 32 B sectors over 20 GB, "
-                                              "the probe's load instruction"}},
+                                       "peak_gathers_per_s": gathers, "peak_inserts_per_s": rmw,
+                                       "floor_ms": floor_ms, "frac": floor_ms / kms,
+                                       "how": "floor = inserts / insert-like rate + other probes / gather "
+                                              "rate (gpx_random_insert_probe, gpx_random_gather_probe: "
+                                              "random 32 B buckets over 20 GB); frac = floor / kernel time"}},
         "clocks": clk,
         # per run: init, the exploration launches, one relaunch test after each, set hash
         "gpu_launches": sum((2 if not args.no_graph else 1) * x["launches"] + 2 for x in results),

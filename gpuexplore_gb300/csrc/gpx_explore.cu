@@ -1227,8 +1227,27 @@ __global__ void random_gather_kernel(const uint32_t *buf, unsigned long long nse
 }
 } // namespace gpx
 
-extern "C" int gpx_random_gather_probe(int device, uint64_t bytes, double *gathers_per_s) {
-    if (!gathers_per_s || bytes < (1u << 20)) return GPX_ERR_INVALID;
+// An insert's access: read a random 32-byte bucket, then a 128-bit CAS on its
+// first slot against what was read (the sector is dirtied and later written back).
+__global__ void random_insert_kernel(uint32_t *buf, unsigned long long nsec, int iters, unsigned long long seed) {
+    unsigned long long tid = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    for (int i = 0; i < iters; i++) {
+        unsigned long long s = __umul64hi(mix64(seed ^ (tid * 0x9E3779B97F4A7C15ull + (unsigned)i)), nsec);
+        uint32_t w[8];
+        ld256_cg(buf + 8 * s, w);
+        const unsigned long long lo = (unsigned long long)w[0] | ((unsigned long long)w[1] << 32);
+        const unsigned long long hi = (unsigned long long)w[2] | ((unsigned long long)w[3] << 32);
+        unsigned long long olo, ohi;
+        cas128(buf + 8 * s, lo, hi, lo + 1ull, hi, olo, ohi);
+    }
+}
+
+namespace {
+
+// Random-access rate over a `bytes` buffer: mode 0 gathers 32-byte sectors,
+// mode 1 makes insert-like read + CAS accesses.  Best of three timed launches.
+int random_access_probe(int device, uint64_t bytes, int mode, double *per_s) {
+    if (!per_s || bytes < (1u << 20)) return GPX_ERR_INVALID;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPX_ERR_NO_GPU;
     GPX_CUDA(cudaSetDevice(device));
@@ -1252,7 +1271,10 @@ extern "C" int gpx_random_gather_probe(int device, uint64_t bytes, double *gathe
     float best = 1e30f;
     for (int rep = 0; rep < 4; rep++) {
         cudaEventRecord(a);
-        random_gather_kernel<<<blocks, threads>>>(buf, bytes / 32, iters, 0x5851F42D4C957F2Dull + rep, sink);
+        if (mode == 0)
+            random_gather_kernel<<<blocks, threads>>>(buf, bytes / 32, iters, 0x5851F42D4C957F2Dull + rep, sink);
+        else // the dirty sectors of one launch are written back during the next
+            random_insert_kernel<<<blocks, threads>>>(buf, bytes / 32, iters, 0x5851F42D4C957F2Dull + rep);
         cudaEventRecord(b);
         cudaEventSynchronize(b);
         float ms = 0;
@@ -1266,9 +1288,20 @@ extern "C" int gpx_random_gather_probe(int device, uint64_t bytes, double *gathe
     cudaFree(buf);
     cudaFree(sink);
     if (e != cudaSuccess) return GPX_ERR_CUDA;
-    *gathers_per_s = (double)blocks * threads * iters / (best * 1e-3);
+    *per_s = (double)blocks * threads * iters / (best * 1e-3);
     return GPX_OK;
 }
+
+} // namespace
+
+extern "C" int gpx_random_insert_probe(int device, uint64_t bytes, double *inserts_per_s) {
+    return random_access_probe(device, bytes, 1, inserts_per_s);
+}
+
+extern "C" int gpx_random_gather_probe(int device, uint64_t bytes, double *gathers_per_s) {
+    return random_access_probe(device, bytes, 0, gathers_per_s);
+}
+
 
 // ======================================================= allocation-free entry point
 //

@@ -26,7 +26,7 @@ EXPORTS = [
     "gpx_status_string", "gpx_abi_version", "gpx_device_info_get", "gpx_options_init", "gpx_model_load",
     "gpx_model_load_file", "gpx_model_from_words", "gpx_model_info_get", "gpx_model_free", "gpx_explore",
     "gpx_explorer_create", "gpx_explorer_run", "gpx_explorer_set_model", "gpx_explorer_destroy",
-    "gpx_result_free", "gpx_explorer_dump", "gpx_explore_noalloc", "gpx_random_gather_probe",
+    "gpx_result_free", "gpx_explorer_dump", "gpx_explore_noalloc", "gpx_random_gather_probe", "gpx_random_insert_probe",
     "gpx_selftest_bounded_wait", "gpx_batch_options_init", "gpx_batch_job_init", "gpx_batch_explore",
     "gpx_explorer_set_por_model", "gpx_explorer_set_por_log", "gpx_explorer_get_por_log",
     "gpx_train_options_init", "gpx_por_train", "gpx_por_grad",
@@ -180,6 +180,7 @@ def load(path: str = LIB) -> C.CDLL:
     lib.gpx_explore_noalloc.argtypes = [vp, C.POINTER(Options), C.POINTER(C.c_uint64), C.c_uint32,
                                         C.POINTER(Result)]
     lib.gpx_random_gather_probe.argtypes = [i, C.c_uint64, C.POINTER(C.c_double)]
+    lib.gpx_random_insert_probe.argtypes = [i, C.c_uint64, C.POINTER(C.c_double)]
     lib.gpx_selftest_bounded_wait.argtypes = [i, C.c_uint64, C.POINTER(C.c_uint64)]
     lib.gpx_explorer_set_por_model.argtypes = [vp, C.POINTER(PorModel)]
     lib.gpx_explorer_set_por_log.argtypes = [vp, C.c_uint64, C.c_uint32]
@@ -405,6 +406,16 @@ def random_gather_rate(device: int = 0, nbytes: int = 20 << 30) -> float:
     rc = load().gpx_random_gather_probe(device, nbytes, C.byref(v))
     if rc != GPX_OK:
         raise GpxError(rc, "random gather probe")
+    return v.value
+
+
+def random_insert_rate(device: int = 0, nbytes: int = 20 << 30) -> float:
+    """Sustained insert-like accesses per second (read a random 32-byte bucket,
+    CAS its first slot) over an `nbytes` buffer: the ceiling of table inserts."""
+    v = C.c_double()
+    rc = load().gpx_random_insert_probe(device, nbytes, C.byref(v))
+    if rc != GPX_OK:
+        raise GpxError(rc, "random insert probe")
     return v.value
 
 

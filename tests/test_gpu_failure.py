@@ -41,3 +41,13 @@ def test_invalid_launch_shape(gpu, tmp_path):
     r = gpu.explore(path, check=False, threads=48)  # not a multiple of 32
     assert r["rc"] == 6
     _still_works(gpu, tmp_path)
+
+
+def test_random_access_probes(gpu):
+    """The two random-access ceilings the bench reports: gathers of random
+    32-byte sectors, and insert-like read + CAS accesses (slower: each dirties
+    a sector that is written back)."""
+    g = gpu.random_gather_rate(0, 1 << 30)
+    i = gpu.random_insert_rate(0, 1 << 30)
+    assert 1e9 < g < 1e12 and 1e9 < i < 1e12
+    assert i < 1.5 * g
