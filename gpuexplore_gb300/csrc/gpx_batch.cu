@@ -168,7 +168,8 @@ static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char 
     P.por_model = I->por_model;
     P.learned = I->por_model ? 1u : 0u;
     P.por_kind = I->por_kind;
-    Explorer<K128, MODE> E(P, I->model, *(WarpScratch<K128, MODE> *)raw);
+    // claims of a few states: each lane evaluates its own pair's rules
+    Explorer<K128, MODE, false> E(P, I->model, *(WarpScratch<K128, MODE> *)raw);
     uint32_t B = WarpScratch<K128, MODE>::kPairs / E.M.n;
     B = B > 32 ? 32 : (B < 1 ? 1 : B);
     if (B > claim) B = (uint32_t)claim; // small claims: one batch per claim, spread over warps

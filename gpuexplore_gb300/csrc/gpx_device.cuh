@@ -88,8 +88,8 @@ struct Params {
     gpx_por_log_row *log;
     unsigned long long *log_count;
     unsigned long long log_cap;
-    // the run's key generation, written by the host before the run (null: 0)
-    const unsigned long long *gen;
+    // tagged slots: the generation counter the init kernel steps (null: untagged)
+    unsigned long long *gen;
     // plain mode: per store position, the participants of the move that first
     // inserted the state (0: none); null disables commuting-move pruning
     uint32_t *label;
@@ -620,7 +620,10 @@ static __device__ __forceinline__ uint32_t float_key(float f) {
 
 // ------------------------------------------------------------- the kernel
 
-template <class K, int MODE> struct Explorer {
+// QUEUE: phase A queues rule items across chunks (the explore kernel's large
+// batches); otherwise each lane evaluates its own pair's rules, which keeps
+// the small batches of the many-network kernel short.
+template <class K, int MODE, bool QUEUE = true> struct Explorer {
     const Params &P;
     MView M;
     WarpScratch<K, MODE> &ws;
@@ -738,11 +741,16 @@ template <class K, int MODE> struct Explorer {
     // its action enabled; its successors (the product of the members' targets)
     // are added to the pair's count unless pruned.
     __device__ void eval_rule(uint32_t i, uint32_t r, bool check) {
-        const uint32_t n = M.n;
-        const uint32_t g = i / n, p = i - g * n;
+        const uint32_t g = i / M.n, p = i - g * M.n;
         const K key = ws.keys[g];
         uint32_t s;
-        const uint32_t *rec = M.state_rec(key, p, s);
+        eval_rule(i, g, p, key, M.state_rec(key, p, s), r, check);
+    }
+
+    // ... for pair i = (state g, process p) whose key and record are at hand
+    __device__ void eval_rule(uint32_t i, uint32_t g, uint32_t p, const K &key, const uint32_t *rec, uint32_t r,
+                              bool check) {
+        const uint32_t n = M.n;
         const uint32_t k = M.lrule(rec[R_ROFF] + r);
         const uint32_t mask = M.rmask(k), act = M.ract(k);
         bool hit1 = false;
@@ -837,6 +845,8 @@ template <class K, int MODE> struct Explorer {
                     if (MODE == MODE_POR) atomicOr(&ws.prov[g], 1u << p);
                 }
                 if (safety && check && p == n - 1 && (rec[R_FLAGS] & 1u)) st.violation = 1;
+                if (!QUEUE)
+                    for (uint32_t x = 0; x < rcnt; x++) eval_rule(i, g, p, key, rec, x, check);
             }
             g += q32;
             p += r32;
@@ -844,6 +854,7 @@ template <class K, int MODE> struct Explorer {
                 p -= n;
                 g++;
             }
+            if (!QUEUE) continue;
             uint32_t incl = rcnt;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {

@@ -207,7 +207,9 @@ template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_k
 
 // Reset the control block to level 0 = {initial state} and insert the
 // all-zero initial state (GPUexplore.cu:668-682).
-template <class K> __global__ void init_kernel(Params P, unsigned int first_phase) {
+// Tagged slots: the run's generation is the device counter *P.gen stepped by
+// one, or 1 when the table was just zeroed (`cleared`).
+template <class K> __global__ void init_kernel(Params P, unsigned int first_phase, unsigned int cleared) {
     Ctrl *c = P.ctrl;
     for (unsigned int i = threadIdx.x; i < sizeof(Ctrl) / 4; i += blockDim.x) ((unsigned int *)c)[i] = 0;
     __syncthreads();
@@ -217,7 +219,10 @@ template <class K> __global__ void init_kernel(Params P, unsigned int first_phas
     c->nlevels = 1;
     c->claim = 1;
     c->phase = first_phase;
-    c->tag = P.gen ? (unsigned int)*P.gen : 0u;
+    if (P.gen) {
+        c->tag = cleared ? 1u : (unsigned int)*P.gen + 1u;
+        *P.gen = c->tag;
+    }
     K key = KT<K>::initial(c->tag);
     unsigned int probes = 0;
     find_or_insert<K>((K *)P.table, P.nbuckets, key, KT<K>::hash(key, P.seed), probes);
@@ -318,7 +323,7 @@ const char *kStatusStrings[] = {"ok",
 
 struct KernelSet {
     void (*explore[3])(Params);
-    void (*init)(Params, unsigned int);
+    void (*init)(Params, unsigned int, unsigned int);
     void (*set_hash)(cudaStream_t, int blocks, const void *store, unsigned long long count,
                      const unsigned long long *count_dev, unsigned long long cap, uint32_t words,
                      unsigned long long *out);
@@ -378,6 +383,7 @@ struct GraphKey {
     uint32_t key_words;
     int collect;
     void *log_count;
+    int clear; // the run zeroes the table first
 };
 constexpr uint32_t kGraphLevels = 4096; // level counts read back by the graph itself
 
@@ -418,9 +424,9 @@ struct gpx_explorer {
     unsigned long long log_cap = 0;
     uint32_t log_every = 0;
     // a run as one CUDA graph (launch_graph), rebuilt when its key changes
-    GraphKey graph_key;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t graph_exec = nullptr;
+    GraphKey graph_key[2];                   // [clear]: runs that zero the table, and the others
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
     cudaStream_t st_body = nullptr;          // captures the body of the launch loop
     unsigned long long *h_levels = nullptr;  // pinned: the first kGraphLevels level counts
     unsigned long long *h_scalar = nullptr;  // pinned: set hash, table count
@@ -428,9 +434,8 @@ struct gpx_explorer {
     size_t saved_fetch = 0;                  // the context's L2 fetch granularity limit before the first run
     bool fetch_saved = false;
     // tagged slots (kind 3): generation of the table's newest keys (0: contents
-    // unknown, clear before the next run), and its pinned source for the device
+    // unknown, clear before the next run); the device steps its own copy
     unsigned int gen = 0;
-    unsigned long long *h_gen = nullptr;
 };
 
 namespace {
@@ -534,7 +539,7 @@ Params make_params(gpx_explorer *ex) {
     P.learned = (ex->o.por == 2 && ex->have_por_model) ? 1u : 0u;
     P.por_kind = por_kind_of(ex->o.por);
     P.por_model = ex->have_por_model ? ex->d_por_model : nullptr;
-    P.gen = ex->d_scalar + 2;
+    P.gen = ex->kind == 3 ? ex->d_scalar + 2 : nullptr;
     if (ex->d_log && ex->log_cap && ex->mode == MODE_PROVISO) {
         P.log = ex->d_log;
         P.log_count = ex->d_log_count;
@@ -549,13 +554,15 @@ int count_blocks(const gpx_explorer *ex) {
 }
 
 void destroy_graph(gpx_explorer *ex) {
-    if (ex->graph_exec) cudaGraphExecDestroy(ex->graph_exec);
-    if (ex->graph) cudaGraphDestroy(ex->graph);
-    ex->graph_exec = nullptr;
-    ex->graph = nullptr;
+    for (int c = 0; c < 2; c++) {
+        if (ex->graph_exec[c]) cudaGraphExecDestroy(ex->graph_exec[c]);
+        if (ex->graph[c]) cudaGraphDestroy(ex->graph[c]);
+        ex->graph_exec[c] = nullptr;
+        ex->graph[c] = nullptr;
+    }
 }
 
-GraphKey graph_key(const gpx_explorer *ex, const Params &P, unsigned int first_phase) {
+GraphKey graph_key(const gpx_explorer *ex, const Params &P, unsigned int first_phase, bool clear) {
     GraphKey k;
     memset(&k, 0, sizeof k);
     k.P = P;
@@ -567,12 +574,12 @@ GraphKey graph_key(const gpx_explorer *ex, const Params &P, unsigned int first_p
     k.key_words = ex->model.dec.key_words;
     k.collect = (ex->o.collect_states || ex->o.verbosity >= 2) ? 1 : 0;
     k.log_count = ex->d_log_count;
+    k.clear = clear ? 1 : 0;
     return k;
 }
 
-// Record one run into a graph on ex->st (the table reset and the generation
-// upload come before it on the stream):
-//   init -> while (more) { exploration launch; relaunch_kernel } -> set hash -> read-back
+// Record one run into a graph on ex->st:
+//   [zero the table] + init -> while (more) { exploration launch; relaunch_kernel } -> set hash -> read-back
 // The loop's condition is set on the device by relaunch_kernel, so a -k run
 // needs no host round trip between launches.
 cudaError_t capture_run(gpx_explorer *ex, const GraphKey &k, cudaGraph_t *out) {
@@ -586,8 +593,10 @@ cudaError_t capture_run(gpx_explorer *ex, const GraphKey &k, cudaGraph_t *out) {
     } while (0)
         Params P = k.P;
         GPX_CAP(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        GPX_CAP(cudaEventRecordWithFlags(ex->ev[0], st, cudaEventRecordExternal));
+        if (k.clear) GPX_CAP(cudaMemsetAsync(ex->d_table, 0, ex->table_bytes, st));
         if (k.log_count) GPX_CAP(cudaMemsetAsync(k.log_count, 0, 8, st));
-        ex->ks.init<<<1, 32, 0, st>>>(P, k.first_phase);
+        ex->ks.init<<<1, 32, 0, st>>>(P, k.first_phase, (unsigned int)k.clear);
         GPX_CAP(cudaGetLastError());
         GPX_CAP(cudaEventRecordWithFlags(ex->ev[1], st, cudaEventRecordExternal));
 
@@ -645,18 +654,22 @@ cudaError_t capture_run(gpx_explorer *ex, const GraphKey &k, cudaGraph_t *out) {
 }
 
 // Run the exploration as one graph launch (built on first use or when the key changed).
-int run_graph(gpx_explorer *ex, const Params &P, unsigned int first_phase) {
-    GraphKey k = graph_key(ex, P, first_phase);
-    if (!ex->graph_exec || memcmp(&k, &ex->graph_key, sizeof k) != 0) {
-        destroy_graph(ex);
+int run_graph(gpx_explorer *ex, const Params &P, unsigned int first_phase, bool clear) {
+    GraphKey k = graph_key(ex, P, first_phase, clear);
+    const int c = clear ? 1 : 0;
+    if (!ex->graph_exec[c] || memcmp(&k, &ex->graph_key[c], sizeof k) != 0) {
+        if (ex->graph_exec[c]) cudaGraphExecDestroy(ex->graph_exec[c]);
+        if (ex->graph[c]) cudaGraphDestroy(ex->graph[c]);
+        ex->graph_exec[c] = nullptr;
+        ex->graph[c] = nullptr;
         if (!ex->st_body) GPX_CUDA(cudaStreamCreateWithFlags(&ex->st_body, cudaStreamNonBlocking));
         if (!ex->h_levels) GPX_CUDA(cudaMallocHost(&ex->h_levels, (size_t)kGraphLevels * 8));
         if (!ex->h_scalar) GPX_CUDA(cudaMallocHost(&ex->h_scalar, 16));
         cudaGraph_t g = nullptr;
         cudaError_t e = capture_run(ex, k, &g);
         if (e == cudaSuccess) {
-            ex->graph = g;
-            e = cudaGraphInstantiate(&ex->graph_exec, g, 0);
+            ex->graph[c] = g;
+            e = cudaGraphInstantiate(&ex->graph_exec[c], g, 0);
         }
         if (e != cudaSuccess) {
             fprintf(stderr, "gpx: building the run graph failed: %s (launch_graph = 0 runs without it)\n",
@@ -665,9 +678,9 @@ int run_graph(gpx_explorer *ex, const Params &P, unsigned int first_phase) {
             cudaGetLastError();
             return GPX_ERR_CUDA;
         }
-        ex->graph_key = k;
+        ex->graph_key[c] = k;
     }
-    GPX_CUDA(cudaGraphLaunch(ex->graph_exec, ex->st));
+    GPX_CUDA(cudaGraphLaunch(ex->graph_exec[c], ex->st));
     GPX_CUDA(cudaStreamSynchronize(ex->st));
     return GPX_OK;
 }
@@ -812,7 +825,6 @@ void gpx_explorer_destroy(gpx_explorer *ex) {
     if (ex->st_body) cudaStreamDestroy(ex->st_body);
     if (ex->h_levels) cudaFreeHost(ex->h_levels);
     if (ex->h_scalar) cudaFreeHost(ex->h_scalar);
-    if (ex->h_gen) cudaFreeHost(ex->h_gen);
     if (ex->d_table) cudaFree(ex->d_table);
     if (ex->d_store) cudaFree(ex->d_store);
     if (ex->d_model) cudaFree(ex->d_model);
@@ -892,7 +904,6 @@ int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_exp
     if (cudaMalloc(&ex->d_scalar, 64) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (cudaMalloc(&ex->d_ctrl, sizeof(Ctrl)) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (cudaMallocHost(&ex->h_ctrl, sizeof(Ctrl)) != cudaSuccess) return fail(GPX_ERR_NOMEM);
-    if (cudaMallocHost(&ex->h_gen, 8) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if ((rc = upload_model(ex)) != GPX_OK) return fail(rc);
     if (cudaStreamSynchronize(ex->st) != cudaSuccess) return fail(GPX_ERR_CUDA);
     *out = ex;
@@ -949,22 +960,20 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     const bool clear = !tagged || ex->gen == 0 || ex->gen >= 255;
     const unsigned int tag = tagged ? (clear ? 1u : ex->gen + 1u) : 0u;
     ex->gen = 0; // until this run has completed
-    *ex->h_gen = tag;
-    GPX_CUDA(cudaEventRecord(ex->ev[0], ex->st));
-    if (clear) GPX_CUDA(cudaMemsetAsync(ex->d_table, 0, ex->table_bytes, ex->st));
-    GPX_CUDA(cudaMemcpyAsync(ex->d_scalar + 2, ex->h_gen, 8, cudaMemcpyHostToDevice, ex->st));
     // -v prints between launches, so it keeps the host loop
     const bool graph = ex->o.launch_graph && ex->o.verbosity <= 0;
     if (graph) {
-        int rc = run_graph(ex, P, first_phase);
+        int rc = run_graph(ex, P, first_phase, clear);
         if (rc != GPX_OK) return rc;
         launches = ex->h_ctrl->launches;
         cudaEventElapsedTime(&setup_ms, ex->ev[0], ex->ev[1]);
         cudaEventElapsedTime(&kernel_ms, ex->ev[1], ex->ev[3]);
         total_ms = kernel_ms;
     } else {
+        GPX_CUDA(cudaEventRecord(ex->ev[0], ex->st));
+        if (clear) GPX_CUDA(cudaMemsetAsync(ex->d_table, 0, ex->table_bytes, ex->st));
         if (ex->d_log_count) GPX_CUDA(cudaMemsetAsync(ex->d_log_count, 0, 8, ex->st));
-        ex->ks.init<<<1, 32, 0, ex->st>>>(P, first_phase);
+        ex->ks.init<<<1, 32, 0, ex->st>>>(P, first_phase, clear ? 1u : 0u);
         GPX_CUDA(cudaGetLastError());
         GPX_CUDA(cudaEventRecord(ex->ev[1], ex->st));
         void (*kern)(Params) = ex->ks.explore[ex->mode];
@@ -1031,7 +1040,6 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     r->slot_bytes = ex->ks.slot_bytes;
     r->blocks = (uint32_t)ex->blocks;
     r->threads = (uint32_t)ex->threads;
-    r->h2d_bytes = 8; // the generation
     r->table_generation = tag;
     r->table_cleared = clear ? 1 : 0;
     if (graph) {
@@ -1444,7 +1452,7 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     GPX_CUDA(cudaMemcpyAsync(base + off_model, model->dec.words.data(), model_bytes, cudaMemcpyHostToDevice, st));
     GPX_CUDA(cudaMemsetAsync(P.table, 0, tb, st));
     GPX_CUDA(cudaMemsetAsync(d_scalar, 0, 64, st));
-    ks.init<<<1, 32, 0, st>>>(P, mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND);
+    ks.init<<<1, 32, 0, st>>>(P, mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND, 1u);
     GPX_CUDA(cudaGetLastError());
     GPX_CUDA(cudaStreamSynchronize(st));
     auto t_kernels = std::chrono::steady_clock::now();
