@@ -46,7 +46,8 @@ struct __align__(128) BInst {
     K128 *store;
     unsigned long long store_cap;
     const uint32_t *model;
-    uint32_t *sel;
+    uint32_t *aux;                  // per store position: the cluster (cycle proviso) or the
+                                    // inserting move's participants (plain, pruning); else null
     unsigned long long *levels;
     unsigned long long max_states;
     uint32_t property, mode;
@@ -160,7 +161,8 @@ static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char 
     P.store = I->store;
     P.store_cap = I->store_cap;
     P.model = I->model;
-    P.sel = I->sel;
+    P.sel = I->mode == MODE_PROVISO ? I->aux : nullptr;
+    P.label = I->mode == MODE_PLAIN ? I->aux : nullptr;
     P.ctrl = &I->ctrl;
     P.seed = BP.seed;
     P.timeout_ns = BP.timeout_ns;
@@ -288,6 +290,7 @@ __global__ void batch_init_kernel(BParams BP, int first_launch) {
     unsigned int probes = 0;
     find_or_insert<K128>(I->table, I->nbuckets, key, KT<K128>::hash(key, BP.seed), probes);
     I->store[0] = key;
+    if (I->mode == MODE_PLAIN && I->aux) I->aux[0] = 0; // the initial state's label: nothing pruned
     I->levels[0] = 1;
 }
 
@@ -332,6 +335,7 @@ namespace {
 
 struct BatchConfig {
     int blocks, threads, claim, kernel_iters, latency_sms;
+    bool prune_commuting;
     double load_factor;
 };
 
@@ -441,7 +445,8 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
         soff[k] = store_bytes;
         store_bytes += cap[k] * sizeof(K128);
         seloff[k] = sel_bytes;
-        if (jobs[idx[k]].por && jobs[idx[k]].cycle_proviso) sel_bytes += (cap[k] * 4 + 255) & ~(size_t)255;
+        const bool aux = jobs[idx[k]].por ? jobs[idx[k]].cycle_proviso != 0 : cfg.prune_commuting;
+        if (aux) sel_bytes += (cap[k] * 4 + 255) & ~(size_t)255;
         moff[k] = model_words;
         model_words += (m->dec.words.size() + 63) & ~(size_t)63;
         memset(&h[k], 0, sizeof(BInst));
@@ -493,7 +498,8 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
         h[k].por_model = (jobs[idx[k]].por == 2) ? d_por : nullptr;
         h[k].table = (K128 *)(d_table + toff[k]);
         h[k].store = (K128 *)(d_store + soff[k]);
-        h[k].sel = h[k].mode == MODE_PROVISO ? (uint32_t *)(d_sel + seloff[k]) : nullptr;
+        const bool aux = h[k].mode == MODE_PROVISO || (h[k].mode == MODE_PLAIN && cfg.prune_commuting);
+        h[k].aux = aux ? (uint32_t *)(d_sel + seloff[k]) : nullptr;
         h[k].model = d_models + moff[k];
         h[k].levels = d_levels + (size_t)k * kBatchLevels;
     }
@@ -606,6 +612,7 @@ void gpx_batch_options_init(gpx_batch_options *o) {
     o->struct_size = sizeof *o;
     o->seed = 0x243F6A8885A308D3ull;
     o->latency_sms = -1;
+    o->prune_commuting = 1;
 }
 
 void gpx_batch_job_init(gpx_batch_job *j) {
@@ -633,6 +640,7 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
     // automatic: about a tenth of the SMs (16 of 152 measured best on config 5, with 8
     // and 24 worse); 0 switches the reservation off
     cfg.latency_sms = opts->latency_sms >= 0 ? opts->latency_sms : prop.multiProcessorCount / 10 + 1;
+    cfg.prune_commuting = opts->prune_commuting != 0;
     if (cfg.threads % 32 || cfg.threads > 256 || cfg.load_factor > 0.95) return GPX_ERR_INVALID;
     const int max_adm = opts->max_admissions > 0 ? opts->max_admissions : 3;
     gpx_batch_stats st;

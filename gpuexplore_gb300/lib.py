@@ -112,7 +112,7 @@ class BatchOptions(C.Structure):
         ("struct_size", C.c_uint32), ("device", C.c_int32), ("blocks", C.c_int32), ("threads", C.c_int32),
         ("claim", C.c_int32), ("kernel_iters", C.c_int32), ("autotune", C.c_int32), ("max_admissions", C.c_int32),
         ("load_factor", C.c_double), ("seed", C.c_uint64), ("por_model", C.c_void_p),
-        ("latency_sms", C.c_int32),
+        ("latency_sms", C.c_int32), ("prune_commuting", C.c_int32),
     ]
 
 

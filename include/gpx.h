@@ -334,6 +334,8 @@ typedef struct {
     const gpx_por_model *por_model; /* for jobs with por == 2 (NULL: plain cample) */
     int32_t latency_sms;    /* SMs that serve the small phases of deep instances (latency-bound) first:
                                -1 (gpx_batch_options_init) = a tenth of the SMs, 0 = none */
+    int32_t prune_commuting; /* 1 (gpx_batch_options_init): plain instances prune commuting moves
+                                (gpx_options.prune_commuting); 0: every successor */
 } gpx_batch_options;
 
 typedef struct {

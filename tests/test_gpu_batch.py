@@ -79,3 +79,13 @@ def test_batch_launch_shapes_and_autotune(gpu, tmp_path):
     items, stats = _check(gpu, tmp_path, cases, autotune=1)
     assert stats["claim"] in (8, 32, 64, 256) and stats["tune_ms"] > 0
     assert stats["p99_ms"] >= stats["p50_ms"] > 0
+
+
+def test_batch_pruning_on_and_off(gpu, tmp_path):
+    """Plain instances prune commuting moves by default (the label array is the
+    per-state array cycle-proviso instances use for clusters); with pruning off
+    every successor is looked up.  Both equal the oracle."""
+    cases = [c for c in _batch_cases(40, 5) if c[1] in ("plain", "deadlock", "safety")][:12]
+    assert len(cases) >= 6
+    _check(gpu, tmp_path, cases)
+    _check(gpu, tmp_path, cases, prune_commuting=0)

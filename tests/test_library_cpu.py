@@ -113,3 +113,4 @@ def test_option_defaults(built):
     b = lib.BatchOptions()
     L.gpx_batch_options_init(lib.C.byref(b))
     assert b.latency_sms == -1 and b.struct_size == lib.C.sizeof(lib.BatchOptions)
+    assert b.prune_commuting == 1
