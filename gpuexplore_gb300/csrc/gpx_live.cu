@@ -16,12 +16,15 @@
 //   until S does not change
 //
 // S is empty iff there is no accepting cycle.  Both steps are frontier
-// sweeps: one thread per frontier state enumerates its successors (the same
-// relation as the exploration kernels: local targets, and for every rule the
-// state's lowest member leads, the product of the members' targets), finds each
-// successor's slot and updates per-slot flags and predecessor counts.
+// sweeps over the successor relation (the exploration kernels' relation: local
+// targets, and for every rule the state's lowest member leads, the product of
+// the members' targets).  When memory allows, the relation is built once as
+// edge lists of store positions -- one pass that generates every successor and
+// finds its slot -- and every sweep then reads lists and per-state flags that
+// stay in L2; otherwise each sweep regenerates successors and looks them up.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 
@@ -118,7 +121,78 @@ __device__ __forceinline__ uint32_t position_of(const K *table, unsigned long lo
     return j == ~0ull ? ~0u : __ldg(index + j);
 }
 
-// count[0]: |S|, count[1]: frontier size, count[2]: next frontier size, count[3]: overflow / missing states
+// count[0]: |S|, count[1]: frontier size, count[2]: next frontier size, count[3]: overflow / missing states,
+// count[4]: edges of the successor lists
+
+// Successors of the state at store position i, as store positions: read from
+// the edge lists when they were built (edges != null), else regenerated and
+// looked up in the table.
+template <class K> struct Succ {
+    const K *table;
+    unsigned long long nb;
+    const uint32_t *index;
+    const K *store;
+    unsigned long long seed;
+    const unsigned long long *beg;
+    const uint32_t *deg;
+    const uint32_t *edges;
+    template <class F> __device__ void each(const MView &M, uint32_t i, F &&f) const {
+        if (edges) {
+            const unsigned long long b = beg[i];
+            const uint32_t d = deg[i];
+            for (uint32_t k = 0; k < d; k++) f(__ldg(edges + b + k));
+            return;
+        }
+        const K key = KT<K>::load(store + i);
+        for_each_successor(M, key, [&](const K &v) { f(position_of(table, nb, index, v, seed)); });
+    }
+};
+
+// Out-degree of every state and the start of its edge list (one atomic per warp).
+template <class K>
+__global__ void live_degree_kernel(const K *store, unsigned long long states, const uint32_t *model, uint32_t *deg,
+                                   unsigned long long *beg, unsigned long long *count) {
+    MView M;
+    M.init(model);
+    const uint32_t lane = threadIdx.x & 31;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long i0 = blockIdx.x * (unsigned long long)blockDim.x + (threadIdx.x & ~31u); i0 < states;
+         i0 += stride) {
+        const unsigned long long i = i0 + lane;
+        uint32_t c = 0;
+        if (i < states) {
+            for_each_successor(M, KT<K>::load(store + i), [&](const K &) { c++; });
+            deg[i] = c;
+        }
+        unsigned long long incl = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(kFull, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        unsigned long long base = 0;
+        if (lane == 31) base = atomicAdd(&count[4], incl);
+        base = __shfl_sync(kFull, base, 31);
+        if (i < states) beg[i] = base + incl - c;
+    }
+}
+
+// The edge lists: every successor's store position.
+template <class K>
+__global__ void live_fill_kernel(const K *table, unsigned long long nb, const uint32_t *index, const K *store,
+                                 unsigned long long states, const uint32_t *model, unsigned long long seed,
+                                 const unsigned long long *beg, uint32_t *edges, unsigned long long *count) {
+    MView M;
+    M.init(model);
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < states;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        unsigned long long e = beg[i];
+        for_each_successor(M, KT<K>::load(store + i), [&](const K &v) {
+            const uint32_t j = position_of(table, nb, index, v, seed);
+            if (j == ~0u) atomicAdd(&count[3], 1ull);
+            edges[e++] = j;
+        });
+    }
+}
 
 // The slot -> store position map, and S := every state.
 template <class K>
@@ -156,17 +230,14 @@ __global__ void live_seed_kernel(const K *store, unsigned long long states, cons
 
 // One forward round: mark the unmarked successors in S of the frontier.
 template <class K>
-__global__ void live_reach_kernel(const K *table, unsigned long long nb, const uint32_t *index, const K *store,
-                                  const uint32_t *model, unsigned long long seed, uint32_t *flag, const uint32_t *front,
+__global__ void live_reach_kernel(Succ<K> S, const uint32_t *model, uint32_t *flag, const uint32_t *front,
                                   unsigned long long nfront, uint32_t *next, unsigned long long cap,
                                   unsigned long long *count) {
     MView M;
     M.init(model);
     for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; t < nfront;
          t += (unsigned long long)gridDim.x * blockDim.x) {
-        const K key = KT<K>::load(store + front[t]);
-        for_each_successor(M, key, [&](const K &v) {
-            const uint32_t j = position_of(table, nb, index, v, seed);
+        S.each(M, front[t], [&](uint32_t j) {
             if (j == ~0u) {
                 atomicAdd(&count[3], 1ull);
                 return;
@@ -194,17 +265,14 @@ __global__ void live_restrict_kernel(unsigned long long states, uint32_t *flag, 
 
 // Predecessor counts inside S (edges counted with multiplicity).
 template <class K>
-__global__ void live_indeg_kernel(const K *table, unsigned long long nb, const uint32_t *index, const K *store,
-                                  unsigned long long states, const uint32_t *model, unsigned long long seed,
-                                  const uint32_t *flag, uint32_t *indeg, unsigned long long *count) {
+__global__ void live_indeg_kernel(Succ<K> S, unsigned long long states, const uint32_t *model, const uint32_t *flag,
+                                  uint32_t *indeg, unsigned long long *count) {
     MView M;
     M.init(model);
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < states;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         if (!(flag[i] & kInSet)) continue;
-        const K key = KT<K>::load(store + i);
-        for_each_successor(M, key, [&](const K &v) {
-            const uint32_t j = position_of(table, nb, index, v, seed);
+        S.each(M, (uint32_t)i, [&](uint32_t j) {
             if (j == ~0u) {
                 atomicAdd(&count[3], 1ull);
                 return;
@@ -225,8 +293,7 @@ __global__ void live_sources_kernel(unsigned long long states, const uint32_t *f
 // One peeling round: remove the frontier from S; successors whose last
 // predecessor in S went form the next frontier.
 template <class K>
-__global__ void live_peel_kernel(const K *table, unsigned long long nb, const uint32_t *index, const K *store,
-                                 const uint32_t *model, unsigned long long seed, uint32_t *flag, uint32_t *indeg,
+__global__ void live_peel_kernel(Succ<K> S, const uint32_t *model, uint32_t *flag, uint32_t *indeg,
                                  const uint32_t *front, unsigned long long nfront, uint32_t *next,
                                  unsigned long long cap, unsigned long long *count) {
     MView M;
@@ -235,9 +302,7 @@ __global__ void live_peel_kernel(const K *table, unsigned long long nb, const ui
          t += (unsigned long long)gridDim.x * blockDim.x) {
         const uint32_t i = front[t];
         flag[i] = 0;
-        const K key = KT<K>::load(store + i);
-        for_each_successor(M, key, [&](const K &v) {
-            const uint32_t j = position_of(table, nb, index, v, seed);
+        S.each(M, i, [&](uint32_t j) {
             if (j == ~0u) {
                 atomicAdd(&count[3], 1ull);
                 return;
@@ -260,6 +325,9 @@ void live_free(LiveScratch *s) {
     cudaFree(s->index);
     cudaFree(s->flag);
     cudaFree(s->indeg);
+    cudaFree(s->deg);
+    cudaFree(s->beg);
+    cudaFree(s->edges);
     cudaFree(s->front[0]);
     cudaFree(s->front[1]);
     cudaFree(s->count);
@@ -301,8 +369,8 @@ int run(const K *table, unsigned long long nb, unsigned long long slots, const K
         }
         s->states = states;
     }
-    if (!s->count) LCUDA(cudaMalloc(&s->count, 4 * 8));
-    unsigned long long h[4];
+    if (!s->count) LCUDA(cudaMalloc(&s->count, 8 * 8));
+    unsigned long long h[5];
     auto read = [&]() -> int {
         LCUDA(cudaMemcpyAsync(h, s->count, sizeof h, cudaMemcpyDeviceToHost, st));
         LCUDA(cudaStreamSynchronize(st));
@@ -320,6 +388,44 @@ int run(const K *table, unsigned long long nb, unsigned long long slots, const K
     LCUDA(cudaGetLastError());
     int rc = read();
     if (rc) return rc;
+    // the successor relation as edge lists of store positions, when it fits in
+    // half of the free memory; otherwise the sweeps regenerate successors
+    Succ<K> S{table, nb, s->index, store, seed, nullptr, nullptr, nullptr};
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && states * 12 < free_b / 4) {
+        if (s->lists_cap < states) {
+            cudaFree(s->deg);
+            cudaFree(s->beg);
+            s->deg = nullptr;
+            s->beg = nullptr;
+            s->lists_cap = 0;
+            LCUDA(cudaMalloc(&s->deg, states * 4));
+            LCUDA(cudaMalloc(&s->beg, states * 8));
+            s->lists_cap = states;
+        }
+        LCUDA(cudaMemsetAsync(s->count, 0, sizeof h, st));
+        live_degree_kernel<K><<<gs, 256, 0, st>>>(store, states, model, s->deg, s->beg, s->count);
+        LCUDA(cudaGetLastError());
+        if ((rc = read())) return rc;
+        const unsigned long long nedges = h[4];
+        cudaMemGetInfo(&free_b, &total_b);
+        if (s->edges_cap >= nedges || nedges * 4 < free_b / 2) {
+            if (s->edges_cap < nedges) {
+                cudaFree(s->edges);
+                s->edges = nullptr;
+                s->edges_cap = 0;
+                LCUDA(cudaMalloc(&s->edges, std::max<unsigned long long>(nedges, 1) * 4));
+                s->edges_cap = nedges;
+            }
+            live_fill_kernel<K><<<gs, 256, 0, st>>>(table, nb, s->index, store, states, model, seed, s->beg,
+                                                    s->edges, s->count);
+            LCUDA(cudaGetLastError());
+            if ((rc = read())) return rc;
+            S.beg = s->beg;
+            S.deg = s->deg;
+            S.edges = s->edges;
+        }
+    }
     unsigned long long size = states;
     for (;;) {
         const unsigned long long before = size;
@@ -332,9 +438,8 @@ int run(const K *table, unsigned long long nb, unsigned long long slots, const K
         unsigned long long nfront = h[1];
         while (nfront) {
             LCUDA(cudaMemsetAsync(s->count + 2, 0, 8, st));
-            live_reach_kernel<K><<<grid_for(nfront), 256, 0, st>>>(table, nb, s->index, store, model, seed, s->flag,
-                                                                   s->front[cur], nfront, s->front[cur ^ 1], cap,
-                                                                   s->count);
+            live_reach_kernel<K><<<grid_for(nfront), 256, 0, st>>>(S, model, s->flag, s->front[cur], nfront,
+                                                                   s->front[cur ^ 1], cap, s->count);
             LCUDA(cudaGetLastError());
             if ((rc = read())) return rc;
             nfront = h[2];
@@ -349,8 +454,7 @@ int run(const K *table, unsigned long long nb, unsigned long long slots, const K
         if (size == 0) break;
         // peel the states with no predecessor in S
         LCUDA(cudaMemsetAsync(s->count, 0, sizeof h, st));
-        live_indeg_kernel<K><<<gs, 256, 0, st>>>(table, nb, s->index, store, states, model, seed, s->flag, s->indeg,
-                                                 s->count);
+        live_indeg_kernel<K><<<gs, 256, 0, st>>>(S, states, model, s->flag, s->indeg, s->count);
         LCUDA(cudaGetLastError());
         live_sources_kernel<<<gs, 256, 0, st>>>(states, s->flag, s->indeg, s->front[0], cap, s->count);
         LCUDA(cudaGetLastError());
@@ -359,9 +463,8 @@ int run(const K *table, unsigned long long nb, unsigned long long slots, const K
         nfront = h[1];
         while (nfront) {
             LCUDA(cudaMemsetAsync(s->count + 2, 0, 8, st));
-            live_peel_kernel<K><<<grid_for(nfront), 256, 0, st>>>(table, nb, s->index, store, model, seed, s->flag,
-                                                                  s->indeg, s->front[cur], nfront, s->front[cur ^ 1],
-                                                                  cap, s->count);
+            live_peel_kernel<K><<<grid_for(nfront), 256, 0, st>>>(S, model, s->flag, s->indeg, s->front[cur],
+                                                                  nfront, s->front[cur ^ 1], cap, s->count);
             LCUDA(cudaGetLastError());
             if ((rc = read())) return rc;
             nfront = h[2];

@@ -15,6 +15,11 @@ struct LiveScratch {
     uint32_t *front[2] = {nullptr, nullptr}; // frontiers of store positions
     unsigned long long *count = nullptr;  // device counters
     unsigned long long slots = 0, states = 0;
+    // the successor relation as edge lists: per state its out-degree and first edge
+    uint32_t *deg = nullptr;
+    unsigned long long *beg = nullptr;
+    uint32_t *edges = nullptr;            // store positions of the successors
+    unsigned long long lists_cap = 0, edges_cap = 0;
 };
 
 void live_free(LiveScratch *s);
