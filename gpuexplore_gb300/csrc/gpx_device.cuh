@@ -753,6 +753,8 @@ template <class K, int MODE, bool QUEUE = true> struct Explorer {
         const uint32_t n = M.n;
         const uint32_t k = M.lrule(rec[R_ROFF] + r);
         const uint32_t mask = M.rmask(k), act = M.ract(k);
+        // expand pass of the cycle proviso (no checks): rules inside the chosen cluster only
+        if (MODE == MODE_PROVISO && !check && (mask & ws.sel[g]) != mask) return;
         bool hit1 = false;
         uint32_t rest = mask, psz = 1;
         while (rest) {
@@ -793,6 +795,8 @@ template <class K, int MODE, bool QUEUE = true> struct Explorer {
                 ws.best[lane] = kFull;
                 ws.vmask[lane] = 0;
                 ws.lbest[lane] = ~0ull;
+                // expand pass of the cycle proviso: the cluster the decide pass chose
+                if (MODE == MODE_PROVISO && !decide) ws.sel[lane] = __ldcg(P.sel + lvl_off + lane);
             } else {
                 // commuting-move pruning: local moves of processes below the
                 // label's lowest participant are generated from another state
@@ -817,7 +821,12 @@ template <class K, int MODE, bool QUEUE = true> struct Explorer {
         for (uint32_t base = 0; base < npairs; base += 32) {
             const uint32_t i = base + lane;
             uint32_t rcnt = 0;
-            if (i < npairs) {
+            if (MODE == MODE_PROVISO && !decide && i < npairs && !(ws.sel[g] >> p & 1u)) {
+                // expand pass of the cycle proviso: processes outside the chosen
+                // cluster make no move (enabledness was checked in the decide pass)
+                ws.appl[i] = 0;
+                ws.pre[i] = 0;
+            } else if (i < npairs) {
                 K key = ws.keys[g];
                 uint32_t s;
                 const uint32_t *rec = M.state_rec(key, p, s);
@@ -893,12 +902,9 @@ template <class K, int MODE, bool QUEUE = true> struct Explorer {
         // B: the cluster each state expands (POR); without the cycle proviso the
         //    proviso bits are plain enabledness (GPUexplore.cu:1395-1397)
         if (MODE == MODE_POR) select_clusters(B, false);
-        if (MODE == MODE_PROVISO && !decide) {
-            if (lane < B) ws.sel[lane] = __ldcg(P.sel + lvl_off + lane);
-            __syncwarp();
-        }
-        if (filter) {
-            // successors of transitions inside the cluster only (GPUexplore.cu:1409, 1541)
+        if (MODE == MODE_POR) {
+            // successors of transitions inside the cluster only (GPUexplore.cu:1409, 1541);
+            // the cycle proviso's expand pass applied its cluster in step A
             for (uint32_t i = lane; i < npairs; i += 32) {
                 uint32_t g = i / n, p = i - g * n;
                 uint32_t sel = ws.sel[g];
