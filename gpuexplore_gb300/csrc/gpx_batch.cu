@@ -170,7 +170,7 @@ static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char 
     P.por_model = I->por_model;
     P.learned = I->por_model ? 1u : 0u;
     P.por_kind = I->por_kind;
-    // claims of a few states: each lane evaluates its own pair's rules
+    // claims of a few states: not the explore kernel's wide-batch machinery
     Explorer<K128, MODE, false> E(P, I->model, *(WarpScratch<K128, MODE> *)raw);
     uint32_t B = WarpScratch<K128, MODE>::kPairs / E.M.n;
     B = B > 32 ? 32 : (B < 1 ? 1 : B);

@@ -19,6 +19,7 @@ namespace gpx {
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr int kPairMax = 256;   // (state, process) pairs staged per warp batch
 constexpr int kPairMaxPor = 160; // ... with POR: its per-pair arrays then fit 4 blocks per SM
+static_assert(kPairMaxPor <= 256, "POR successor owners are stored as 8-bit pair indices");
 constexpr int kMaxProbe = 32;   // buckets probed before reporting the table full
 constexpr uint32_t kMaxLevels = 1u << 20;
 // cluster definitions of the POR modes: static clusters (cample), single-process
@@ -487,6 +488,11 @@ template <class K, int MODE> struct WarpScratch {
     uint32_t clo[kPor];          // per pair: cluster closure
     uint32_t nw[kPor];           // per pair: successors not yet visited (decide pass, for the log)
     uint16_t cand[kPor];         // learned proposal / log: the pairs whose closure is scored
+    // POR modes, while successors are materialised (clo is dead then): the pair
+    // of each successor index, when the batch has at most kOwners successors
+    static constexpr uint32_t kOwners = (MODE == MODE_PLAIN) ? 0u : 4u * kPor;
+    __device__ uint8_t *owner() { return reinterpret_cast<uint8_t *>(clo); }
+    __device__ const uint8_t *owner() const { return reinterpret_cast<const uint8_t *>(clo); }
     static constexpr int kSrc = (MODE == MODE_PLAIN) ? 1 : 32; // per-state arrays of the POR modes
     static constexpr int kLab = (MODE == MODE_PLAIN) ? 32 : 1; // ... and of plain mode
     uint32_t prov[kSrc], sel[32], best[kSrc], vmask[kSrc];
@@ -620,10 +626,12 @@ static __device__ __forceinline__ uint32_t float_key(float f) {
 
 // ------------------------------------------------------------- the kernel
 
-// QUEUE: phase A queues rule items across chunks (the explore kernel's large
-// batches); otherwise each lane evaluates its own pair's rules, which keeps
-// the small batches of the many-network kernel short.
-template <class K, int MODE, bool QUEUE = true> struct Explorer {
+// WIDE: the explore kernel's wide batches -- phase A queues rule items across
+// chunks, and POR modes tabulate each successor's pair.  The many-network
+// kernel's small claims do neither: each lane evaluates its own pair's rules
+// and successors find their pair by binary search, which keeps every claim's
+// latency short.
+template <class K, int MODE, bool WIDE = true> struct Explorer {
     const Params &P;
     MView M;
     WarpScratch<K, MODE> &ws;
@@ -678,14 +686,18 @@ template <class K, int MODE, bool QUEUE = true> struct Explorer {
 
     // Successor number t of the batch (ws.pre holds the per-pair prefix): the
     // pair's local targets first, then the products of the rules it leads.
-    __device__ void materialise(uint32_t t, uint32_t npairs, bool filter, K &out, uint32_t &og,
+    __device__ void materialise(uint32_t t, uint32_t npairs, bool filter, bool owned, K &out, uint32_t &og,
                                 uint32_t &omask) const {
         const uint32_t n = M.n;
         uint32_t lo = 0, hi = npairs;
-        while (hi - lo > 1) {
-            uint32_t mid = (lo + hi) >> 1;
-            if (ws.pre[mid] <= t) lo = mid;
-            else hi = mid;
+        if (owned) {
+            lo = ws.owner()[t];
+        } else {
+            while (hi - lo > 1) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (ws.pre[mid] <= t) lo = mid;
+                else hi = mid;
+            }
         }
         uint32_t sub = t - ws.pre[lo];
         og = lo / n;
@@ -854,7 +866,7 @@ template <class K, int MODE, bool QUEUE = true> struct Explorer {
                     if (MODE == MODE_POR) atomicOr(&ws.prov[g], 1u << p);
                 }
                 if (safety && check && p == n - 1 && (rec[R_FLAGS] & 1u)) st.violation = 1;
-                if (!QUEUE)
+                if (!WIDE)
                     for (uint32_t x = 0; x < rcnt; x++) eval_rule(i, g, p, key, rec, x, check);
             }
             g += q32;
@@ -863,7 +875,7 @@ template <class K, int MODE, bool QUEUE = true> struct Explorer {
                 p -= n;
                 g++;
             }
-            if (!QUEUE) continue;
+            if (!WIDE) continue;
             uint32_t incl = rcnt;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -942,6 +954,14 @@ template <class K, int MODE, bool QUEUE = true> struct Explorer {
         }
         if (lane == 0) ws.pre[npairs] = carry;
         __syncwarp();
+        // POR modes: the pair of every successor index, written once, instead of
+        // a binary search over the prefix sums per successor
+        const bool owned = WIDE && MODE != MODE_PLAIN && carry <= WarpScratch<K, MODE>::kOwners;
+        if (owned) {
+            for (uint32_t i = lane; i < npairs; i += 32)
+                for (uint32_t t = ws.pre[i], e = ws.pre[i + 1]; t < e; t++) ws.owner()[t] = (uint8_t)i;
+            __syncwarp();
+        }
 
         // C: one successor per lane per round, materialised by index, then looked up
         for (uint32_t t0 = 0; t0 < carry; t0 += 32) {
@@ -949,7 +969,7 @@ template <class K, int MODE, bool QUEUE = true> struct Explorer {
             bool valid = t < carry;
             K out;
             uint32_t og = 0, omask = 0;
-            if (valid) materialise(t, npairs, filter, out, og, omask);
+            if (valid) materialise(t, npairs, filter, owned, out, og, omask);
             if (MODE == MODE_PROVISO && decide) {
                 if (valid) {
                     st.lookups++;
