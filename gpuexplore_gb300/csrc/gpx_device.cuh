@@ -19,7 +19,7 @@ namespace gpx {
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr int kPairMax = 256;   // (state, process) pairs staged per warp batch
 constexpr int kPairMaxPor = 160; // ... with POR: its per-pair arrays then fit 4 blocks per SM
-static_assert(kPairMaxPor <= 256, "POR successor owners are stored as 8-bit pair indices");
+static_assert(kPairMax <= 256 && kPairMaxPor <= 256, "successor owners are stored as 8-bit pair indices");
 constexpr int kMaxProbe = 32;   // buckets probed before reporting the table full
 constexpr uint32_t kMaxLevels = 1u << 20;
 // cluster definitions of the POR modes: static clusters (cample), single-process
@@ -489,7 +489,9 @@ template <class K, int MODE> struct WarpScratch {
     uint32_t nw[kPor];           // per pair: successors not yet visited (decide pass, for the log)
     uint16_t cand[kPor];         // learned proposal / log: the pairs whose closure is scored
     // POR modes, while successors are materialised (clo is dead then): the pair
-    // of each successor index, when the batch has at most kOwners successors
+    // of each successor index, when the batch has at most kOwners successors.
+    // (Plain mode keeps the binary search: a 64-entry table of its own measured
+    // 3% slower on the pruned config-2 kernel.)
     static constexpr uint32_t kOwners = (MODE == MODE_PLAIN) ? 0u : 4u * kPor;
     __device__ uint8_t *owner() { return reinterpret_cast<uint8_t *>(clo); }
     __device__ const uint8_t *owner() const { return reinterpret_cast<const uint8_t *>(clo); }
