@@ -39,6 +39,20 @@ def test_cli_matches_oracle(gpu, built, tmp_path, flags, expect):
     assert re.search(r"^Run time: [0-9.]+$", r.stdout, re.M)
 
 
+@pytest.mark.parametrize("prop", ["-d", "-p"])
+def test_cli_no_prune(gpu, built, tmp_path, prop):
+    """--no-prune (every successor looked up) prints the same result lines."""
+    net = gen.random_network(16, nprocs=9, states=(3, 6), outdeg=(1, 2), sync_frac=0.7)
+    path = write_net(net, tmp_path, "m")
+    o = oracle(path, [prop])
+    for extra in ([], ["--no-prune"]):
+        r = _run(built, path, "-q", str(1 << 22), prop, *extra)
+        assert r.returncode == 0, r.stderr
+        assert _count(r.stdout) == o["states"]
+        assert ("deadlock detected!" in r.stdout) == (o["verdict"] == "deadlock")
+        assert ("safety property violation detected!" in r.stdout) == (o["verdict"] == "safety")
+
+
 def test_cli_dump_is_the_visited_set(gpu, built, tmp_path):
     net = gen.random_network(31, nprocs=10, states=(3, 6))
     path = write_net(net, tmp_path, "m")
