@@ -3,6 +3,8 @@ per-level counts and visited set whatever order decides which predecessor
 inserts a state first (the order is shuffled, as races shuffle it on the GPU),
 on networks with local moves only, with many multi-party synchronisations, and
 with clusters."""
+import functools
+import operator
 import random
 
 import pytest
@@ -39,3 +41,39 @@ def test_prunes_most_diamonds():
     net = gen.random_network(3, nprocs=6, states=(3, 5), sync_frac=0.0, safety=False)
     got = ax.explore_pruned(net, random.Random(0), max_states=20_000)
     assert got["pruned"] > 2 * got["generated"]
+
+
+def _por_pruned_states(net):
+    """Cluster POR (no proviso) with the pruning rule applied on top: the
+    combination the kernels do not make."""
+    n = net.nprocs
+    init = tuple([0] * n)
+    label = {init: 0}
+    frontier = [init]
+    while frontier:
+        sel = {s: ax.select_cluster(n, ax.static_clusters(net, s),
+                                    functools.reduce(operator.or_, (m for _, m in ax.successors(net, s)), 0))
+               for s in frontier}
+        nxt = []
+        for s in frontier:
+            lab = label[s]
+            low = (lab & -lab).bit_length() - 1
+            for t, mask in ax.successors(net, s):
+                lead = (mask & -mask).bit_length() - 1
+                if mask & sel[s] != mask or (lab and lead < low and mask & lab == 0):
+                    continue
+                if t not in label:
+                    label[t] = mask
+                    nxt.append(t)
+        frontier = nxt
+    return set(label)
+
+
+def test_unsound_under_por():
+    """Why only plain exploration prunes: a reduced expansion need not contain
+    the commuted path the argument relies on, so pruning inside cluster POR can
+    lose states (here one of four)."""
+    net = gen.random_network(182, nprocs=5, states=(2, 4), outdeg=(1, 2), safety=False)
+    ref = ax.explore(net, por=True)["visited"]
+    got = _por_pruned_states(net)
+    assert got < ref
