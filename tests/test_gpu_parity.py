@@ -88,6 +88,22 @@ def test_full_set_rows(gpu, tmp_path):
     assert got.shape[0] == sum(g["levels"])
 
 
+@pytest.mark.parametrize("flags", ["por_proviso", "stubborn_proviso", "ample_safety", "safety"])
+def test_high_load_eviction_with_reductions(gpu, tmp_path, flags):
+    """Bounded eviction under the cycle proviso (whose decide pass looks keys up
+    after level-close eviction has moved some) with cample, stubborn and ample
+    clusters over thousands of levels, and under the safety check with pruning."""
+    net = gen.random_network(42, nprocs=28, states=(3, 6), outdeg=(1, 2))
+    assert net.firstbit()[-1] > 63
+    path = write_net(net, tmp_path, "dense")
+    cli, kw = FLAGS[flags]
+    o = oracle(path, cli, max_states=150_000)
+    q_words = (int(o["states"] * 1.08) * 16) // 4
+    g = _gpu(gpu, path, kw, max_states=150_000, q_words=q_words, store_states=o["states"] + 64, collect_states=1)
+    _same(o, g)
+    assert g["table_count"] == g["states"]
+
+
 @pytest.mark.parametrize("slots_per_state", [1.06, 1.15])
 def test_high_load_bounded_eviction(gpu, tmp_path, slots_per_state):
     """A table barely larger than the state space: inserts whose probe sequence is
