@@ -36,6 +36,26 @@ def test_liveness_matches_oracle(gpu, tmp_path, name):
         assert g["live_ms"] > 0
 
 
+@pytest.mark.parametrize("name", ["random30", "progress22c"])
+def test_liveness_on_a_full_table(gpu, tmp_path, name):
+    """A table barely larger than the state space: level-close eviction moves
+    keys along their probe sequences, and the check still finds every
+    successor's slot; replays reuse the table by generation."""
+    path = write_net(CASES[name](), tmp_path, name)
+    o = oracle(path, ["-p"])
+    q_words = (int(o["states"] * 1.08) * 16) // 4
+    ex = gpu.Explorer(gpu.Model.from_file(path), gpu.options(property="safety", cycle_proviso=1, q_words=q_words,
+                                                             store_states=o["states"] + 64))
+    try:
+        for _ in range(2):
+            g = ex.run(check=False)
+            assert g["rc"] == 0, g
+            assert g["states"] == o["states"] and g["set_hash"] == o["set_hash"]
+            assert g["verdict"] == o["verdict"] and (g["live_states"] > 0) == (o["verdict"] == "liveness")
+    finally:
+        ex.close()
+
+
 def test_liveness_replay_and_model_switch(gpu, tmp_path):
     """One explorer, alternating violating and non-violating models."""
     nets = [gen.progress_network(5, cyclic=True), gen.progress_network(5), gen.progress_network(6, cyclic=True)]
