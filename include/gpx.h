@@ -188,10 +188,11 @@ int gpx_selftest_bounded_wait(int device, uint64_t timeout_ns, uint64_t *waited_
  * gathers per second.  Allocates and frees the buffer itself. */
 int gpx_random_gather_probe(int device, uint64_t bytes, double *gathers_per_s);
 
-/* The ceiling of hash-table inserts: random 32-byte buckets of a `bytes`-sized
- * device buffer, each read and then updated by a 128-bit CAS on its first slot
- * (the insert's access: one random sector read, one dirty sector written back),
- * in accesses per second. */
+/* Insert roofline probe (no reference counterpart; a measurement aid): random
+ * 32-byte buckets of a `bytes`-sized device buffer, each read and then updated
+ * by a 128-bit CAS on its first slot -- the insert's access, one random sector
+ * read and one dirty sector written back -- in accesses per second.  Allocates
+ * and frees the buffer itself. */
 int gpx_random_insert_probe(int device, uint64_t bytes, double *inserts_per_s);
 
 /* Exploration that allocates no memory -- no counterpart in the reference.
