@@ -145,26 +145,35 @@ typedef struct {
     char name[256];
 } gpx_device_info;
 
+/* Text of a gpx_status (the reference prints these conditions and exits,
+ * GPUexplore.cu:522-528, 1985, 2001, 2164-2166). */
 const char *gpx_status_string(int status);
+/* GPX_ABI_VERSION of the library (no reference counterpart). */
 int gpx_abi_version(void);
 /* GPX_ERR_NO_GPU when no CUDA device is present (GPUexplore.cu:1999-2003). */
 int gpx_device_info_get(int device, gpx_device_info *info);
 
+/* Defaults of the options (the reference's argv defaults, GPUexplore.cu:102-104, 1805-1883;
+ * blocks/threads/levels per launch default to the whole GPU in one launch). */
 void gpx_options_init(gpx_options *opts);
 
 /* Load <path_without_ext>.gpf, appending the extension like GPUexplore.cu:1814-1815. */
 int gpx_model_load(const char *path_without_ext, gpx_model **out);
-/* Load a gpf file by its exact path. */
+/* Load a gpf file by its exact path (the reading of GPUexplore.cu:1885-1987). */
 int gpx_model_load_file(const char *path, gpx_model **out);
-/* Parse gpf integers already in host memory (one integer per gpf line). */
+/* Parse gpf integers already in host memory, one integer per gpf line (the same
+ * reading without a file, GPUexplore.cu:1885-1987). */
 int gpx_model_from_words(const uint32_t *words, size_t nwords, gpx_model **out);
 int gpx_model_info_get(const gpx_model *model, gpx_model_info *info);
+/* Release a model (no reference counterpart: the reference never releases its arrays). */
 void gpx_model_free(gpx_model *model);
 
 /* One-shot exploration: allocate, explore, free (the reference's main, GPUexplore.cu:1989-2172). */
 int gpx_explore(const gpx_model *model, const gpx_options *opts, gpx_result *result);
 
-/* Reusable explorer: device memory (hash table, state store) is allocated once and
+/* Reusable explorer: the one-shot exploration split into allocation (create),
+ * runs (the reset and exploration loop of GPUexplore.cu:2091-2142, each call) and
+ * release (destroy).  Device memory (hash table, state store) is allocated once and
  * each run resets it, so repeated explorations pay no allocation. */
 int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_explorer **out);
 int gpx_explorer_run(gpx_explorer *ex, gpx_result *result);
@@ -173,6 +182,8 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *result);
 int gpx_explorer_set_model(gpx_explorer *ex, const gpx_model *model);
 void gpx_explorer_destroy(gpx_explorer *ex);
 
+/* Release the arrays of a result (no reference counterpart: the reference prints its
+ * results, GPUexplore.cu:2144-2172). */
 void gpx_result_free(gpx_result *result);
 
 /* Failure-detection self-test (no reference counterpart): runs the bounded
