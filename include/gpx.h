@@ -145,8 +145,8 @@ typedef struct {
     char name[256];
 } gpx_device_info;
 
-/* Text of a gpx_status (the reference prints these conditions and exits,
- * GPUexplore.cu:522-528, 1985, 2001, 2164-2166). */
+/* Text of a status code; the reference prints these conditions and exits
+ * (GPUexplore.cu:522-528, 1985, 2001, 2164-2166). */
 const char *gpx_status_string(int status);
 /* GPX_ABI_VERSION of the library (no reference counterpart). */
 int gpx_abi_version(void);
