@@ -115,9 +115,18 @@ static __device__ __forceinline__ void prefetch_l2(const void *p) {
     asm volatile("prefetch.global.L2 [%0];" : : "l"(p));
 }
 
+// One 32-byte bucket in one load.  Each vector element is read single-copy
+// atomically, so a slot is never seen half-written: 32-bit elements for
+// 32-bit slots, 64-bit elements for 64-bit slots and the halves of 128-bit ones.
 static __device__ __forceinline__ void ld256_cg(const void *p, uint32_t (&w)[8]) {
     asm volatile("ld.global.cg.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
+                 : "l"(p));
+}
+
+static __device__ __forceinline__ void ld256_cg(const void *p, unsigned long long (&d)[4]) {
+    asm volatile("ld.global.cg.v4.u64 {%0,%1,%2,%3}, [%4];"
+                 : "=l"(d[0]), "=l"(d[1]), "=l"(d[2]), "=l"(d[3])
                  : "l"(p));
 }
 
@@ -174,10 +183,10 @@ template <> struct KT<K64> {
     __device__ static uint64_t hash(const K64 &k, uint64_t seed) { return mix64(k.v ^ seed); }
     __device__ static K64 cas(K64 *p, K64 cmp, K64 val) { return {atomicCAS(&p->v, cmp.v, val.v)}; }
     __device__ static void bucket(const K64 *b, K64 (&s)[kSlots]) {
-        uint32_t w[8];
-        ld256_cg(b, w);
+        unsigned long long d[4];
+        ld256_cg(b, d);
 #pragma unroll
-        for (int j = 0; j < 4; j++) s[j].v = (unsigned long long)w[2 * j] | ((unsigned long long)w[2 * j + 1] << 32);
+        for (int j = 0; j < 4; j++) s[j].v = d[j];
     }
     __device__ static K64 load(const K64 *p) { return {__ldcg(&p->v)}; }
     __device__ static void words(const K64 &k, uint32_t (&w)[4]) {
@@ -239,12 +248,12 @@ static __device__ __forceinline__ void cas128(void *p, unsigned long long clo, u
 
 static __device__ __forceinline__ void bucket128(const void *b, unsigned long long (&lo)[2],
                                                  unsigned long long (&hi)[2]) {
-    uint32_t w[8];
-    ld256_cg(b, w);
-    lo[0] = (unsigned long long)w[0] | ((unsigned long long)w[1] << 32);
-    hi[0] = (unsigned long long)w[2] | ((unsigned long long)w[3] << 32);
-    lo[1] = (unsigned long long)w[4] | ((unsigned long long)w[5] << 32);
-    hi[1] = (unsigned long long)w[6] | ((unsigned long long)w[7] << 32);
+    unsigned long long d[4];
+    ld256_cg(b, d);
+    lo[0] = d[0];
+    hi[0] = d[1];
+    lo[1] = d[2];
+    hi[1] = d[3];
 }
 
 // 128-bit slots hold 63 state bits in each 64-bit half (bit 63 of both halves
