@@ -45,7 +45,7 @@ BUDGET = 100_000_000
 Q_WORDS = 5_000_000_000
 CPU_SAMPLE_BUDGET = 10_000_000  # stops after BFS level 8 (about 4.2e7 states)
 WORKLOAD = "config-2 random gpf network (16 procs + monitor, seed 2024), -d, BFS to 1e8-state budget"
-KERNEL_BUILD = "guided-claims-v7-prune-rulequeue"  # names the kernel version a committed traffic capture belongs to
+KERNEL_BUILD = "guided-claims-v8-prune-v4u64"  # names the kernel version a committed traffic capture belongs to
 
 
 def measured_peaks():
