@@ -37,7 +37,7 @@ def test_pruned_equals_unpruned(gpu, tmp_path, name, flags):
         _same(o, runs[prune])
     on, off = runs[1], runs[0]
     assert off["pruned"] == 0
-    assert on["lookups"] + on["pruned"] == off["lookups"]
+    assert on["lookups"] + on["pruned"] == off["lookups"] == o["generated"]  # every successor, once
     assert on["inserts"] == off["inserts"] and on["expanded"] == off["expanded"]
     if name == "local" and on["states"] > 1000:
         assert on["pruned"] > 2 * on["lookups"]
