@@ -152,16 +152,17 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
             for (uint32_t k = o1; k < o2; k++) {
                 if (k >= g.nr_trans) return "transition range past proc_trans";
                 uint32_t e = g.proc_trans[k];
-                std::vector<uint32_t> ts;
+                uint32_t ts[32], nts = 0;             // nslots <= 30
                 for (uint32_t i = 0; i < nslots; i++) {  // slots hold target+1 (GPUexplore.cu:159)
                     uint32_t t = (e >> (1 + g.bits_act + i * w)) & ((1u << w) - 1u);
                     if (!t) break;
-                    ts.push_back(t - 1);
+                    ts[nts++] = t - 1;
                 }
-                if (ts.empty()) return "transition entry without targets";
+                if (!nts) return "transition entry without targets";
                 std::vector<uint32_t> &dst =
                     (e & 1u) ? rec.sync[(e >> 1) & ((1u << g.bits_act) - 1u)] : rec.local;
-                for (uint32_t t : ts) {
+                for (uint32_t x = 0; x < nts; x++) {
+                    const uint32_t t = ts[x];
                     if (std::find(dst.begin(), dst.end(), t) == dst.end()) dst.push_back(t);
                     if (!seen[t]) {
                         seen[t] = 1;
@@ -172,25 +173,30 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
         }
         nstates[p] = maxs + 1;
         ps[p].resize(nstates[p]);
-        for (auto &kv : dec) ps[p][kv.first] = kv.second;
+        for (auto &kv : dec) ps[p][kv.first] = std::move(kv.second);
     }
     if (state_bits > (uint32_t)kMaxStateBits) return "UNSUPPORTED: state vector wider than 126 bits";
 
     // rules, and per (p, s) the rules p leads (lowest member) for actions p has enabled
     std::vector<uint32_t> rule_mask, rule_act;
-    std::map<uint32_t, std::pair<uint32_t, uint32_t>> rules_range; // action -> [first, count)
-    std::set<uint32_t> actions;
+    std::vector<uint32_t> actions; // ascending, each once
     for (uint32_t p = 0; p < n; p++)
         for (auto &r : ps[p])
-            for (auto &kv : r.sync) actions.insert(kv.first);
+            for (auto &kv : r.sync) actions.push_back(kv.first);
+    std::sort(actions.begin(), actions.end());
+    actions.erase(std::unique(actions.begin(), actions.end()), actions.end());
+    std::vector<std::pair<uint32_t, uint32_t>> ranges(actions.size()); // per action: [first rule, count)
+    auto rules_range = [&](uint32_t a) -> const std::pair<uint32_t, uint32_t> & {
+        return ranges[std::lower_bound(actions.begin(), actions.end(), a) - actions.begin()];
+    };
     std::vector<uint32_t> masks;
-    for (uint32_t a : actions) {
-        std::string err = rules_of(a, &masks);
+    for (size_t i = 0; i < actions.size(); i++) {
+        std::string err = rules_of(actions[i], &masks);
         if (!err.empty()) return err;
-        rules_range[a] = {(uint32_t)rule_mask.size(), (uint32_t)masks.size()};
+        ranges[i] = {(uint32_t)rule_mask.size(), (uint32_t)masks.size()};
         for (uint32_t m : masks) {
             rule_mask.push_back(m);
-            rule_act.push_back(a);
+            rule_act.push_back(actions[i]);
         }
     }
 
@@ -222,8 +228,8 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
                 sent.push_back(kv.first);
                 sent.push_back(toff);
                 sent.push_back((uint32_t)kv.second.size());
-                sent.push_back(has1 | (rules_range[kv.first].first << 1)); // + first rule of the action
-                auto rr = rules_range[kv.first];
+                sent.push_back(has1 | (rules_range(kv.first).first << 1)); // + first rule of the action
+                auto rr = rules_range(kv.first);
                 for (uint32_t k = rr.first; k < rr.first + rr.second; k++) {
                     uint32_t m = rule_mask[k];
                     if (m >> p & 1u) cl0 |= m; // GPUexplore.cu:1616-1624
