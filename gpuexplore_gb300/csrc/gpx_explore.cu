@@ -259,19 +259,28 @@ template <class K>
 __global__ void set_hash_kernel(const K *store, unsigned long long count, const unsigned long long *count_dev,
                                 unsigned long long cap, uint32_t words, unsigned long long *out) {
     if (count_dev) count = *count_dev < cap ? *count_dev : cap;
-    unsigned long long acc = 0;
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < count;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
+    auto term = [words](const K &key) {
         uint32_t w[4];
-        KT<K>::words(KT<K>::load(store + i), w);
+        KT<K>::words(key, w);
         uint64_t h = 0x9E3779B97F4A7C15ull;
         for (uint32_t j = 0; j < words; j += 2) {
             uint64_t cc = w[j];
             if (j + 1 < words) cc |= (uint64_t)w[j + 1] << 32;
             h = mix64(h ^ cc);
         }
-        acc += h;
+        return h;
+    };
+    unsigned long long acc = 0;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < count; i += 4 * stride) { // four loads in flight before any hashing
+        K k[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) k[u] = KT<K>::load(store + i + u * stride);
+#pragma unroll
+        for (int u = 0; u < 4; u++) acc += term(k[u]);
     }
+    for (; i < count; i += stride) acc += term(KT<K>::load(store + i));
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
 }
