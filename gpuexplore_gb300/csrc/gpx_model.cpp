@@ -5,8 +5,6 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
-#include <map>
-#include <set>
 
 namespace gpx {
 
@@ -127,7 +125,15 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
     // decode every (p, s) reachable in p's LTS from local state 0
     struct PS {
         std::vector<uint32_t> local;
-        std::map<uint32_t, std::vector<uint32_t>> sync;
+        std::vector<std::pair<uint32_t, std::vector<uint32_t>>> sync; // ascending action
+        std::vector<uint32_t> &targets_of(uint32_t a) {
+            auto it = std::lower_bound(sync.begin(), sync.end(), a,
+                                       [](const std::pair<uint32_t, std::vector<uint32_t>> &x, uint32_t v) {
+                                           return x.first < v;
+                                       });
+            if (it == sync.end() || it->first != a) it = sync.insert(it, {a, {}});
+            return it->second;
+        }
     };
     std::vector<std::vector<PS>> ps(n);
     std::vector<uint32_t> nstates(n);
@@ -136,11 +142,14 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
         const uint32_t nfields = nwords * per_off;
         const uint32_t *base = g.proc_offsets.data() + g.proc_offsets_start[p];
         const uint32_t w = g.bits_state[p], nslots = (31 - g.bits_act) / w;
-        std::vector<int> seen(1u << w, 0);
+        // every reachable local state s needs offset fields s and s+1, so state
+        // indices are bounded by the input, whatever bits_state allows
+        if (nfields < 2) return "transition offsets missing for a reachable local state";
+        std::vector<char> seen(nfields, 0);
         std::vector<uint32_t> todo{0};
         seen[0] = 1;
         uint32_t maxs = 0;
-        std::map<uint32_t, PS> dec;
+        std::vector<PS> dec(nfields);
         while (!todo.empty()) {
             uint32_t s = todo.back();
             todo.pop_back();
@@ -160,10 +169,11 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
                 }
                 if (!nts) return "transition entry without targets";
                 std::vector<uint32_t> &dst =
-                    (e & 1u) ? rec.sync[(e >> 1) & ((1u << g.bits_act) - 1u)] : rec.local;
+                    (e & 1u) ? rec.targets_of((e >> 1) & ((1u << g.bits_act) - 1u)) : rec.local;
                 for (uint32_t x = 0; x < nts; x++) {
                     const uint32_t t = ts[x];
                     if (std::find(dst.begin(), dst.end(), t) == dst.end()) dst.push_back(t);
+                    if (t + 1 >= nfields) return "transition offsets missing for a reachable local state";
                     if (!seen[t]) {
                         seen[t] = 1;
                         todo.push_back(t);
@@ -173,7 +183,8 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
         }
         nstates[p] = maxs + 1;
         ps[p].resize(nstates[p]);
-        for (auto &kv : dec) ps[p][kv.first] = std::move(kv.second);
+        for (uint32_t st = 0; st <= maxs; st++)
+            if (seen[st]) ps[p][st] = std::move(dec[st]);
     }
     if (state_bits > (uint32_t)kMaxStateBits) return "UNSUPPORTED: state vector wider than 126 bits";
 
