@@ -114,3 +114,22 @@ def test_option_defaults(built):
     L.gpx_batch_options_init(lib.C.byref(b))
     assert b.latency_sms == -1 and b.struct_size == lib.C.sizeof(lib.BatchOptions)
     assert b.prune_commuting == 1
+
+
+def test_wide_local_state_fields_decode_in_bounded_memory(built):
+    """A process whose declared bits_state far exceeds its state count: the
+    decoder's reachability array is bounded by the gpf's offset fields, not by
+    2^bits_state (which would be 2^27 entries here)."""
+    import time
+    from gpuexplore_gb300 import lib
+    net = gen.ring(1, nprocs=3, nstates=3)
+    net.bits_state = lambda: [27, 2, 2]
+    words = gpf.encode(net)
+    t0 = time.perf_counter()
+    m = lib.Model.from_words(words)
+    elapsed = time.perf_counter() - t0
+    try:
+        assert m.info().state_bits == 31
+    finally:
+        m.close()
+    assert elapsed < 0.1
