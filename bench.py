@@ -15,14 +15,17 @@ value    states / device time of the step (table reset + exploration kernels,
          CUDA events on the launching stream; the model is already resident)
 e2e      the same metric through the C ABI with host buffers: every step parses
          the gpf words from host memory, copies the model to the device
-         (gpx_explorer_set_model) and reads the results back (gpx_explorer_run)
+         (gpx_explorer_set_model) and reads the results back (gpx_explorer_run;
+         the visited-set hash, a check, is off as in the library's defaults)
 roofline dominant kernel (explore_kernel): algorithmic bytes per launch --
          32 B per hash lookup, 32 B per insert, 2 x 4*sv_nints B per expanded
          state -- over its CUDA-event duration, against the measured HBM peak
 cpu_baseline / --impl reference
          the CPU oracle (a port of the reference's semantics; the reference has
-         no CPU path) with all host threads, on the first 9 BFS levels of the
-         same network
+         no CPU path) with all host threads on the whole workload (all 10
+         levels); its states, level counts and visited-set hash must equal the
+         GPU run's (cpu_baseline.parity).  A single-thread figure on a named
+         sample (the first 9 levels) is reported beside it.
 
 Multi-GPU (torchrun): replicas -- each rank explores its own copy; the job
 value is the sum of states over the max step time across ranks ("weak").
@@ -40,10 +43,12 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-SEED = 2024
-BUDGET = 100_000_000
-Q_WORDS = 5_000_000_000
-CPU_SAMPLE_BUDGET = 10_000_000  # stops after BFS level 8 (about 4.2e7 states)
+from gpuexplore_gb300 import workloads as W  # noqa: E402
+
+SEED = W.CONFIG2_SEED
+BUDGET = W.CONFIG2_BUDGET
+Q_WORDS = W.CONFIG2_Q_WORDS
+CPU_SAMPLE_BUDGET = W.CONFIG2_SAMPLE_BUDGET  # the first 9 BFS levels (38.8M states)
 WORKLOAD = "config-2 random gpf network (16 procs + monitor, seed 2024), -d, BFS to 1e8-state budget"
 KERNEL_BUILD = "guided-claims-v8-prune-v4u64"  # names the kernel version a committed traffic capture belongs to
 
@@ -57,9 +62,17 @@ def measured_peaks():
 
 
 def make_network_words():
-    from gpuexplore_gb300 import gen, gpf
-    net = gen.random_network(SEED)
+    from gpuexplore_gb300 import gpf
+    net = W.config2_network()
     return net, gpf.encode(net)
+
+
+def workload_config(budget, q_words, states, levels):
+    """The `config` object both arms print: the workload only (network,
+    property, budget, table size) and the size of its result."""
+    return {"workload": WORKLOAD, "property": "deadlock (-d)", "budget": budget, "q_words": q_words,
+            "table_gb": q_words * 4 / 1e9, "states": states, "levels": levels,
+            "l2": "inputs larger than L2 (20 GB hash table, reset every step)"}
 
 
 class ClockSampler:
@@ -142,8 +155,18 @@ def cpu_oracle_run(path, threads, budget):
     return json.loads(out.stdout)
 
 
+def cpu_single_thread(path):
+    """The oracle on one thread over the named sample (the first 9 levels)."""
+    o = cpu_oracle_run(path, 1, CPU_SAMPLE_BUDGET)
+    return {"value": o["states"] / o["seconds"], "unit": "states/s", "cores": 1, "seconds": o["seconds"],
+            "sample": f"first {len(o['levels'])} BFS levels ({o['states']} states) of the same network"}
+
+
 def run_reference(args, rank, world):
-    """The CPU oracle (the reference's semantics on host cores) on a bounded sample."""
+    """The reference's algorithm on the host cores: the CPU oracle (the reference
+    has no CPU path of its own) with every host thread, on the whole workload.
+    Warm-up steps run the first 9 levels only (the CPU has nothing to warm
+    beyond its caches and page tables); timed steps run all 10."""
     if rank != 0:
         return
     from gpuexplore_gb300 import build, gpf
@@ -155,18 +178,24 @@ def run_reference(args, rank, world):
         gpf.write(net, path)
         for _ in range(args.warmup):
             cpu_oracle_run(path, threads, CPU_SAMPLE_BUDGET)
-        secs, states = [], 0
+        secs, results = [], []
         for _ in range(args.steps):
-            o = cpu_oracle_run(path, threads, CPU_SAMPLE_BUDGET)
+            o = cpu_oracle_run(path, threads, args.budget)
             secs.append(o["seconds"])
-            states = o["states"]
-    v = states / (sum(secs) / len(secs))
-    sample = f"first {len(o['levels'])} BFS levels ({states} states) of the same network"
+            results.append(o)
+        single = cpu_single_thread(path)
+    o = results[-1]
+    for x in results:  # deterministic whatever the thread schedule
+        assert (x["states"], x["levels"], x["set_hash"]) == (o["states"], o["levels"], o["set_hash"])
+    v = o["states"] / (sum(secs) / len(secs))
+    sample = (f"the whole workload: {len(o['levels'])} BFS levels, {o['states']} states, on {threads} host threads "
+              f"(OpenMP); warm-up steps on the first 9 levels")
     line = {"impl": "reference", "metric": "new states/s", "value": v, "unit": "states/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(secs) / len(secs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": sample, "cpu_threads": threads},
-            "cpu_baseline": {"value": v, "unit": "states/s", "cores": threads, "kind": "port", "sample": sample},
+            "config": workload_config(args.budget, args.q_words, o["states"], len(o["levels"])),
+            "cpu_baseline": {"value": v, "unit": "states/s", "cores": threads, "kind": "port", "sample": sample,
+                             "set_hash": o["set_hash"], "single_thread": single},
             "e2e": {"value": v, "unit": "states/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -263,12 +292,13 @@ def run_other_workload(args, local):
         return
     if args.workload in ("config1", "config3"):
         if args.workload == "config1":
-            nets = [gen.ring(s) for s in range(1, 11)]
-            kw = dict(property="deadlock", q_words=1 << 22)
+            nets = W.config1_networks()
+            kw = dict(W.PROPERTY_FLAGS["deadlock"][1], q_words=W.CONFIG1_Q_WORDS)
             desc = "config-1 rings of 8 processes x 5 states, seeds 1-10, -d, 2^22-word table"
         else:
-            nets = [gen.clustered(s, nprocs=24) for s in range(1, 4)]
-            kw = dict(por=1, cycle_proviso=1, q_words=2_500_000_000, max_states=min(args.budget, 20_000_000))
+            nets = W.config3_networks()
+            kw = dict(W.PROPERTY_FLAGS["por_proviso"][1], q_words=W.CONFIG3_Q_WORDS,
+                      max_states=min(args.budget, W.CONFIG3_BUDGET))
             desc = "config-3 clustered networks (24 processes, 4-6 clusters), seeds 1-3, --por --cycle-proviso"
         models = [lib.Model.from_words(gpf.encode(n)) for n in nets]
         ex = lib.Explorer(models[0], lib.options(device=local, **kw))
@@ -330,11 +360,13 @@ def run_other_workload(args, local):
             jobs.append({"property": "deadlock" if k % 2 == 0 else "safety",
                          "por": 2 if (k // 2) % 2 else 0, "cycle_proviso": 1 if (k // 2) % 2 else 0,
                          "max_states": int(10 ** rng.uniform(3, 7))})
-        # the warm-up call autotunes claim size, block size and load factor; timed calls reuse them
+        # the warm-up call autotunes claim size, block size, load factor and claims per
+        # launch; timed calls reuse them
         tuned = {}
         for w in range(max(1, args.warmup)):
             _, st = lib.batch_explore(models, jobs, autotune=1 if w == 0 else 0, por_model=por_model, **tuned)
-            tuned = {"claim": st["claim"], "threads": st["threads"], "load_factor": st["load_factor"]}
+            tuned = {"claim": st["claim"], "threads": st["threads"], "load_factor": st["load_factor"],
+                     "kernel_iters": st["kernel_iters"]}
         dev, states, p50, p99 = 0.0, 0, [], []
         for _ in range(args.steps):
             items, st = lib.batch_explore(models, jobs, por_model=por_model, **tuned)
@@ -348,7 +380,8 @@ def run_other_workload(args, local):
                                         "the learned proposal and the cycle proviso, one persistent launch",
                             "states_per_step": states // args.steps, "p50_ms": statistics.median(p50),
                             "p99_ms": statistics.median(p99), "claim": st["claim"], "threads": st["threads"],
-                            "load_factor": st["load_factor"], "tune_ms": st["tune_ms"],
+                            "load_factor": st["load_factor"], "kernel_iters": st["kernel_iters"],
+                            "tune_ms": st["tune_ms"], "instances_by_slot_32_64_128": st["instances_by_slot"],
                             "admissions_max": max(it["admissions"] for it in items),
                             "failed": sum(1 for it in items if it["status"] != 0)})
     print(json.dumps(line), flush=True)
@@ -402,9 +435,11 @@ def main():
     net, words = make_network_words()
     sv_nints = (net.firstbit()[-1] + 1 + 31) // 32  # the reference's words per vector
     model = lib.Model.from_words(words)
-    opts = lib.options(property="deadlock", q_words=args.q_words, max_states=args.budget,
-                       store_states=args.store_states, device=local, launch_graph=0 if args.no_graph else 1)
-    ex = lib.Explorer(model, opts)
+    base = dict(property="deadlock", q_words=args.q_words, max_states=args.budget, store_states=args.store_states,
+                device=local, launch_graph=0 if args.no_graph else 1)
+    # Device-timed runs compute the visited-set hash after the timed interval, so
+    # that every run can be checked against the others and against the oracle.
+    ex = lib.Explorer(model, lib.options(set_hash=1, **base))
 
     def barrier():
         if dist:
@@ -420,21 +455,30 @@ def main():
         dev_ms.append(r["setup_ms"] + r["kernel_ms"])
         ker_ms.append(r["kernel_ms"])
         results.append(r)
-    # end to end through the C ABI from host buffers
-    e2e_s = []
+    ex.close()
+    # End to end through the C ABI from host buffers, with the library's defaults
+    # (no set hash): parse the gpf words, upload the model, explore, read back.
+    ex2 = lib.Explorer(model, lib.options(**base))
+    for _ in range(args.warmup):
+        ex2.run()
+    e2e_s, e2e_runs = [], []
     h2d = len(words) * 4
     for _ in range(args.steps):
         t0 = time.perf_counter()
         m = lib.Model.from_words(words)
-        ex.set_model(m)
-        r2 = ex.run()
+        ex2.set_model(m)
+        r2 = ex2.run()
         e2e_s.append(time.perf_counter() - t0)
+        e2e_runs.append(r2)
         m.close()
+    ex2.close()
     barrier()
     clk = clocks.stop()
     r = results[-1]
-    for x in results + [r2]:
+    for x in results:
         assert x["states"] == r["states"] and x["levels"] == r["levels"] and x["set_hash"] == r["set_hash"]
+    for x in e2e_runs:
+        assert x["states"] == r["states"] and x["levels"] == r["levels"]
     # The table is reset by generation: each run's keys carry a new 8-bit tag and
     # older slots read as free, so one run in 255 zeroes the 20 GB table.  That
     # clear is charged to every step, amortised over the runs it serves.
@@ -471,16 +515,14 @@ def main():
         "metric": "new states/s", "value": value, "unit": "states/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded gpf generator)",
-        "config": {"workload": WORKLOAD, "states": r["states"], "levels": len(r["levels"]),
-                   "budget": args.budget, "table_gb": args.q_words * 4 / 1e9, "slot_bytes": r["slot_bytes"],
-                   "blocks": r["blocks"],
-                   "threads": r["threads"], "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (20 GB table, reset every step)",
+        "config": workload_config(args.budget, args.q_words, r["states"], len(r["levels"])),
+        "parallelism": f"replicas x{world}",
+        "launch": {"slot_bytes": r["slot_bytes"], "blocks": r["blocks"], "threads": r["threads"],
                    "table_reset": {"how": "generation tag in every slot" if r["table_generation"] else "clear",
                                    "clear_ms": clear_ms, "runs_per_clear": per_clear,
                                    "amortised_ms_per_step": amortised}},
         "e2e": {"value": e2e, "unit": "states/s", "h2d_bytes_per_step": h2d + r2["h2d_bytes"],
-                "d2h_bytes_per_step": r2["d2h_bytes"]},
+                "d2h_bytes_per_step": r2["d2h_bytes"], "set_hash": "off (library default)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                      "peak_source": f"{peak_kind} hbm_gbs", "kernel": "explore_kernel",
@@ -494,25 +536,34 @@ def main():
                                               "rate (gpx_random_insert_probe, gpx_random_gather_probe: "
                                               "random 32 B buckets over 20 GB); frac = floor / kernel time"}},
         "clocks": clk,
-        # per run: init, the exploration launches, one relaunch test after each, set hash
-        "gpu_launches": sum((2 if not args.no_graph else 1) * x["launches"] + 2 for x in results),
+        # per device-timed run: init, then per exploration launch the launch itself, the placement
+        # kernel (returns at once unless a level overflowed) and, in the graph, the relaunch test;
+        # then the set hash
+        "gpu_launches": sum((3 if not args.no_graph else 2) * x["launches"] + 2 for x in results),
         "hash_probe_gbs": 32 * r["probes"] / (kms / 1000.0) / 1e9,
     }
+    parity_ok = True
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from gpuexplore_gb300 import gpf
         threads = os.cpu_count() or 1
         with tempfile.TemporaryDirectory() as d:
             path = os.path.join(d, "c2.gpf")
             gpf.write(net, path)
-            o = cpu_oracle_run(path, threads, CPU_SAMPLE_BUDGET)
+            o = cpu_oracle_run(path, threads, args.budget)
+            single = cpu_single_thread(path)
+        # the oracle checks the GPU run: same states, per-level counts and visited set
+        parity_ok = (o["states"], o["levels"], o["set_hash"]) == (r["states"], r["levels"], r["set_hash"])
         line["cpu_baseline"] = {"value": o["states"] / o["seconds"], "unit": "states/s", "cores": threads,
                                 "kind": "port",
-                                "sample": f"first {len(o['levels'])} BFS levels ({o['states']} states)"}
+                                "sample": f"the whole workload: {len(o['levels'])} BFS levels, {o['states']} states "
+                                          f"on {threads} host threads (OpenMP)",
+                                "parity": parity_ok, "set_hash": o["set_hash"], "single_thread": single}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ex.close()
     if dist:
         dist.destroy_process_group()
+    if not parity_ok:
+        sys.exit("bench: the GPU run's visited set differs from the oracle's")
 
 
 if __name__ == "__main__":

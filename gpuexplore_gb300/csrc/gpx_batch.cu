@@ -9,7 +9,9 @@
 // kernel (Explorer in gpx_device.cuh), and report the states they completed;
 // the warp that completes the last chunk of a level closes it and publishes the
 // next epoch.  No grid-wide barrier is needed, so small instances finish and
-// free the GPU for large ones.  All instances use 128-bit slots.
+// free the GPU for large ones.  Each instance has the slot width its state
+// vector needs (32, 64 or 128 bits), so a small network's partition holds two
+// or four times the states of a 128-bit one in the same bytes.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -41,9 +43,9 @@ struct __align__(128) BInst {
     unsigned long long completed[2];
     unsigned long long finish_ns;
     // set up by the host
-    K128 *table;
+    void *table;                    // slots of the instance's width (kind)
     unsigned long long nbuckets;
-    K128 *store;
+    void *store;
     unsigned long long store_cap;
     const uint32_t *model;
     uint32_t *aux;                  // per store position: the cluster (cycle proviso) or the
@@ -51,8 +53,11 @@ struct __align__(128) BInst {
     unsigned long long *levels;
     unsigned long long max_states;
     uint32_t property, mode;
-    uint32_t por_kind, pad_kind;    // POR_CAMPLE / POR_AMPLE / POR_STUBBORN (job por 1-2 / 3 / 4)
+    uint32_t por_kind;              // POR_CAMPLE / POR_AMPLE / POR_STUBBORN (job por 1-2 / 3 / 4)
+    uint32_t kind;                  // slot width: 0 = 32, 1 = 64, 2 = 128 bits
     const gpx_por_model *por_model; // learned proposal (job por == 2), else null
+    void *overflow;                 // keys whose probe sequence was full during the current level,
+    unsigned long long overflow_cap; // placed with eviction by the warp that closes it
 };
 
 struct BGlobal {
@@ -150,8 +155,9 @@ static __device__ void close_instance(const BParams &BP, BInst *I, unsigned int 
     atomicExch(&I->ticket, (unsigned long long)(e + 1) << 40);
 }
 
-template <int MODE>
-static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char *raw, unsigned long long lo,
+// Not inlined: each (slot width, mode) path gets its own register allocation.
+template <class K, int MODE>
+static __device__ __noinline__ void process_claim(const BParams &BP, BInst *I, unsigned char *raw, unsigned long long lo,
                                      unsigned long long off, unsigned long long cnt, unsigned long long claim,
                                      bool decide) {
     Params P;
@@ -160,6 +166,8 @@ static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char 
     P.nbuckets = I->nbuckets;
     P.store = I->store;
     P.store_cap = I->store_cap;
+    P.overflow = I->overflow;
+    P.overflow_cap = I->overflow_cap;
     P.model = I->model;
     P.sel = I->mode == MODE_PROVISO ? I->aux : nullptr;
     P.label = I->mode == MODE_PLAIN ? I->aux : nullptr;
@@ -171,8 +179,8 @@ static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char 
     P.learned = I->por_model ? 1u : 0u;
     P.por_kind = I->por_kind;
     // claims of a few states: not the explore kernel's wide-batch machinery
-    Explorer<K128, MODE, false> E(P, I->model, *(WarpScratch<K128, MODE> *)raw);
-    uint32_t B = WarpScratch<K128, MODE>::kPairs / E.M.n;
+    Explorer<K, MODE, false> E(P, I->model, *(WarpScratch<K, MODE> *)raw);
+    uint32_t B = WarpScratch<K, MODE>::kPairs / E.M.n;
     B = B > 32 ? 32 : (B < 1 ? 1 : B);
     if (B > claim) B = (uint32_t)claim; // small claims: one batch per claim, spread over warps
     for (unsigned long long b = off; b < off + cnt; b += B) {
@@ -181,6 +189,25 @@ static __device__ void process_claim(const BParams &BP, BInst *I, unsigned char 
         E.batch(lo + b, n, b, decide, (uint32_t)(left < B ? left : B));
     }
     E.flush_stats(); // appends the staged new states before the chunk is reported
+}
+
+// A claim of instance I with its slot width and mode.
+template <class K>
+static __device__ void run_claim(const BParams &BP, BInst *I, unsigned char *raw, unsigned long long lo,
+                                 unsigned long long off, unsigned long long cnt, unsigned long long claim, bool decide) {
+    if (I->mode == MODE_PLAIN)
+        process_claim<K, MODE_PLAIN>(BP, I, raw, lo, off, cnt, claim, false);
+    else if (I->mode == MODE_POR)
+        process_claim<K, MODE_POR>(BP, I, raw, lo, off, cnt, claim, false);
+    else
+        process_claim<K, MODE_PROVISO>(BP, I, raw, lo, off, cnt, claim, decide);
+}
+
+// The level's overflowed keys of instance I, placed by the closing warp.
+template <class K> static __device__ __noinline__ void place_instance(const BParams &BP, BInst *I, unsigned long long over,
+                                                         uint32_t lane) {
+    place_list_warp<K>((K *)I->table, I->nbuckets, (K *)I->store, I->mode == MODE_PLAIN ? I->aux : nullptr,
+                       I->store_cap, (const K *)I->overflow, over, &I->ctrl, BP.seed, lane);
 }
 
 __global__ void __launch_bounds__(256, 3) batch_kernel(BParams BP) {
@@ -234,16 +261,35 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(BParams BP) {
             if (cur >= n) continue;
             unsigned long long cnt = (n - cur) < claim ? (n - cur) : claim;
             bool decide = L.phase == PH_DECIDE;
-            if (I->mode == MODE_PLAIN)
-                process_claim<MODE_PLAIN>(BP, I, raw, L.lo, cur, cnt, claim, false);
-            else if (I->mode == MODE_POR)
-                process_claim<MODE_POR>(BP, I, raw, L.lo, cur, cnt, claim, false);
+            if (I->kind == 0)
+                run_claim<K32>(BP, I, raw, L.lo, cur, cnt, claim, decide);
+            else if (I->kind == 1)
+                run_claim<K64>(BP, I, raw, L.lo, cur, cnt, claim, decide);
             else
-                process_claim<MODE_PROVISO>(BP, I, raw, L.lo, cur, cnt, claim, decide);
+                run_claim<K128>(BP, I, raw, L.lo, cur, cnt, claim, decide);
             __threadfence();
-            if (lane == 0) {
-                unsigned long long d = atomicAdd(&I->completed[e2 & 1], cnt) + cnt;
-                if (d == n) close_instance(BP, I, e2);
+            unsigned long long d = 0;
+            if (lane == 0) d = atomicAdd(&I->completed[e2 & 1], cnt) + cnt;
+            if (__shfl_sync(kFull, d, 0) == n) {
+                // every chunk of the epoch is done: the instance is quiescent.  Keys
+                // whose probe sequence was full are placed with eviction first.
+                __threadfence();
+                Ctrl *c = &I->ctrl;
+                const unsigned long long over = vload(&c->overflow_count);
+                if (over) {
+                    if (over <= I->overflow_cap && !vload(&c->error)) {
+                        if (I->kind == 0)
+                            place_instance<K32>(BP, I, over, lane);
+                        else if (I->kind == 1)
+                            place_instance<K64>(BP, I, over, lane);
+                        else
+                            place_instance<K128>(BP, I, over, lane);
+                    } else if (lane == 0)
+                        set_error(c, GPX_ERR_TABLE_FULL); // re-admitted with a larger partition
+                    if (lane == 0) c->overflow_count = 0;
+                    __threadfence();
+                }
+                if (lane == 0) close_instance(BP, I, e2);
             }
             __syncwarp();
             worked = true;
@@ -280,16 +326,25 @@ __global__ void batch_relaunch_kernel(BGlobal *g, uint32_t count, cudaGraphCondi
     cudaGraphSetConditional(loop, more);
 }
 
+template <class K> static __device__ void insert_initial(BInst *I, unsigned long long seed) {
+    const K key = KT<K>::initial(0);
+    unsigned int probes = 0;
+    find_or_insert<K>((K *)I->table, I->nbuckets, key, KT<K>::hash(key, seed), probes);
+    ((K *)I->store)[0] = key;
+}
+
 // Initial state of every instance (GPUexplore.cu:668-682) and the launch clock.
 __global__ void batch_init_kernel(BParams BP, int first_launch) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0 && first_launch) BP.g->start_ns = globaltimer();
     if (i >= BP.count) return;
     BInst *I = &BP.inst[i];
-    K128 key = KT<K128>::initial(0);
-    unsigned int probes = 0;
-    find_or_insert<K128>(I->table, I->nbuckets, key, KT<K128>::hash(key, BP.seed), probes);
-    I->store[0] = key;
+    if (I->kind == 0)
+        insert_initial<K32>(I, BP.seed);
+    else if (I->kind == 1)
+        insert_initial<K64>(I, BP.seed);
+    else
+        insert_initial<K128>(I, BP.seed);
     if (I->mode == MODE_PLAIN && I->aux) I->aux[0] = 0; // the initial state's label: nothing pruned
     I->levels[0] = 1;
 }
@@ -303,7 +358,12 @@ __global__ void batch_hash_kernel(const BInst *inst, uint32_t count, const uint3
         unsigned long long acc = 0;
         for (unsigned long long j = threadIdx.x; j < cnt; j += blockDim.x) {
             uint32_t w[4];
-            KT<K128>::words(KT<K128>::load(I->store + j), w);
+            if (I->kind == 0)
+                KT<K32>::words(KT<K32>::load((const K32 *)I->store + j), w);
+            else if (I->kind == 1)
+                KT<K64>::words(KT<K64>::load((const K64 *)I->store + j), w);
+            else
+                KT<K128>::words(KT<K128>::load((const K128 *)I->store + j), w);
             uint64_t h = 0x9E3779B97F4A7C15ull;
             for (uint32_t k = 0; k < words[i]; k += 2) {
                 uint64_t cc = w[k];
@@ -346,6 +406,23 @@ struct Outcome {
     double completion_ms;
     std::vector<uint64_t> levels;
 };
+
+constexpr unsigned long long kInstOverflow = 1024; // overflowed keys an instance can place per level
+constexpr uint32_t kSlotBytes[3] = {4, 8, 16};
+
+// Slot width of an instance: the narrowest that holds its state vector and the
+// occupancy bit of each 32/64-bit half (as in a single-network table).
+uint32_t slot_kind(const gpx_model *m) {
+    const uint32_t bits = m->dec.state_bits;
+    return bits <= 31 ? 0u : (bits <= 63 ? 1u : 2u);
+}
+
+// Device bytes per admitted state: table slots at the load factor, the store
+// slot and the per-state cluster / label word.
+double bytes_per_state(const gpx_model *m, double load_factor) {
+    const double sb = kSlotBytes[slot_kind(m)];
+    return sb / load_factor + sb + 4.0;
+}
 
 // Admission estimate: the state budget with a margin for the last level's
 // overshoot, bounded by the product of the local state counts.
@@ -435,15 +512,20 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
     std::vector<uint32_t> words_per(count);
     size_t table_bytes = 0, store_bytes = 0, sel_bytes = 0, model_words = 0;
     std::vector<size_t> toff(count), soff(count), seloff(count), moff(count);
+    std::vector<size_t> ooff(count);
+    size_t over_bytes = 0;
     for (uint32_t k = 0; k < count; k++) {
         const gpx_model *m = models[idx[k]];
+        const uint32_t kind = slot_kind(m), sb = kSlotBytes[kind], per_bucket = 32 / sb;
         uint64_t slots = (uint64_t)((double)cap[k] / cfg.load_factor) + 4;
-        uint64_t nb = (slots + 1) / 2;
+        uint64_t nb = (slots + per_bucket - 1) / per_bucket;
         nb = (nb + 1) & ~1ull; // even: buckets are probed in pairs
         toff[k] = table_bytes;
         table_bytes += nb * 32;
         soff[k] = store_bytes;
-        store_bytes += cap[k] * sizeof(K128);
+        store_bytes += (cap[k] * sb + 255) & ~(size_t)255;
+        ooff[k] = over_bytes;
+        over_bytes += kInstOverflow * sb;
         seloff[k] = sel_bytes;
         const bool aux = jobs[idx[k]].por ? jobs[idx[k]].cycle_proviso != 0 : cfg.prune_commuting;
         if (aux) sel_bytes += (cap[k] * 4 + 255) & ~(size_t)255;
@@ -458,6 +540,7 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
         h[k].property = (uint32_t)prop_k;
         h[k].mode = jobs[idx[k]].por ? (jobs[idx[k]].cycle_proviso ? MODE_PROVISO : MODE_POR) : MODE_PLAIN;
         h[k].por_kind = jobs[idx[k]].por == 3 ? POR_AMPLE : (jobs[idx[k]].por == 4 ? POR_STUBBORN : POR_CAMPLE);
+        h[k].kind = kind;
         h[k].ctrl.store_count = 1;
         h[k].ctrl.nlevels = 1;
         h[k].ctrl.hi = 1;
@@ -466,7 +549,7 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
         h[k].lvl[0].phase = h[k].mode == MODE_PROVISO ? PH_DECIDE : PH_EXPAND;
         words_per[k] = m->dec.key_words;
     }
-    unsigned char *d_table = nullptr, *d_store = nullptr, *d_sel = nullptr;
+    unsigned char *d_table = nullptr, *d_store = nullptr, *d_sel = nullptr, *d_over = nullptr;
     uint32_t *d_models = nullptr, *d_words = nullptr;
     unsigned long long *d_levels = nullptr, *d_hash = nullptr;
     BInst *d_inst = nullptr;
@@ -488,6 +571,7 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
     BCUDA(cudaMalloc(&d_table, std::max<size_t>(table_bytes, 256)));
     BCUDA(cudaMalloc(&d_store, std::max<size_t>(store_bytes, 256)));
     BCUDA(cudaMalloc(&d_sel, std::max<size_t>(sel_bytes, 256)));
+    BCUDA(cudaMalloc(&d_over, std::max<size_t>(over_bytes, 256)));
     BCUDA(cudaMalloc(&d_models, std::max<size_t>(model_words * 4, 256)));
     BCUDA(cudaMalloc(&d_words, count * 4));
     BCUDA(cudaMalloc(&d_levels, (size_t)count * kBatchLevels * 8));
@@ -496,12 +580,14 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
     BCUDA(cudaMalloc(&d_g, sizeof(BGlobal)));
     for (uint32_t k = 0; k < count; k++) {
         h[k].por_model = (jobs[idx[k]].por == 2) ? d_por : nullptr;
-        h[k].table = (K128 *)(d_table + toff[k]);
-        h[k].store = (K128 *)(d_store + soff[k]);
+        h[k].table = d_table + toff[k];
+        h[k].store = d_store + soff[k];
         const bool aux = h[k].mode == MODE_PROVISO || (h[k].mode == MODE_PLAIN && cfg.prune_commuting);
         h[k].aux = aux ? (uint32_t *)(d_sel + seloff[k]) : nullptr;
         h[k].model = d_models + moff[k];
         h[k].levels = d_levels + (size_t)k * kBatchLevels;
+        h[k].overflow = d_over + ooff[k];
+        h[k].overflow_cap = kInstOverflow;
     }
     BCUDA(cudaMemset(d_table, 0, std::max<size_t>(table_bytes, 256)));
     BCUDA(cudaMemset(d_hash, 0, count * 8));
@@ -587,6 +673,7 @@ done:
     cudaFree(d_table);
     cudaFree(d_store);
     cudaFree(d_sel);
+    cudaFree(d_over);
     cudaFree(d_models);
     cudaFree(d_words);
     cudaFree(d_levels);
@@ -670,9 +757,8 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
     {
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return GPX_ERR_CUDA;
-        const double per_state = 16.0 / cfg.load_factor + 16.0 + 4.0;
         double want = 0;
-        for (uint32_t i : todo) want += (double)cap[i] * per_state;
+        for (uint32_t i : todo) want += (double)cap[i] * bytes_per_state(models[i], cfg.load_factor);
         const double room = 0.7 * (double)free_b;
         if (want > room)
             for (uint32_t i : todo) cap[i] = std::max<uint64_t>(1024, (uint64_t)((double)cap[i] * room / want));
@@ -715,6 +801,23 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
                         bestc = c;
                     }
                 }
+        // then the claims per warp per launch (0: one launch until every instance is
+        // done; otherwise warps leave after that many claims and the device-side
+        // loop relaunches, which redistributes them over the SMs)
+        for (int iters : {0, 64, 512}) {
+            if (iters == bestc.kernel_iters) continue;
+            BatchConfig c = bestc;
+            c.kernel_iters = iters;
+            std::vector<Outcome> o;
+            float ms = 0;
+            uint32_t l = 0;
+            if (run_launch(opts->device, prop, c, opts->seed, models, jobs, sample, scap, d_por, &o, &ms, &l) ==
+                    GPX_OK &&
+                ms < best) {
+                best = ms;
+                bestc = c;
+            }
+        }
         cfg = bestc;
         st.tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
@@ -726,9 +829,8 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
         {
             size_t free_b = 0, total_b = 0;
             cudaMemGetInfo(&free_b, &total_b);
-            const double per_state = 16.0 / cfg.load_factor + 16.0 + 4.0;
             double want = 0;
-            for (uint32_t i : todo) want += (double)cap[i] * per_state;
+            for (uint32_t i : todo) want += (double)cap[i] * bytes_per_state(models[i], cfg.load_factor);
             const double room = 0.7 * (double)free_b;
             double scale = want > room ? room / want : 1.0;
             for (uint32_t i : todo) c2.push_back(std::max<uint64_t>(1024, (uint64_t)((double)cap[i] * scale)));
@@ -752,6 +854,7 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
             it.set_hash = o.set_hash;
             it.capacity = o.capacity;
             it.completion_ms = o.completion_ms;
+            it.slot_bytes = kSlotBytes[slot_kind(models[i])];
             if (adm == 1 && o.status == GPX_OK) completion.push_back(o.completion_ms);
             if (level_counts && level_capacity)
                 for (uint32_t l = 0; l < std::min<uint32_t>(level_capacity, (uint32_t)o.levels.size()); l++)
@@ -774,6 +877,9 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
     st.threads = cfg.threads;
     st.blocks = cfg.blocks;
     st.load_factor = cfg.load_factor;
+    st.kernel_iters = cfg.kernel_iters;
+    for (uint32_t i = 0; i < count; i++)
+        if (items[i].slot_bytes) st.instances_by_slot[items[i].slot_bytes == 4 ? 0 : (items[i].slot_bytes == 8 ? 1 : 2)]++;
     if (stats) *stats = st;
     return rc;
 }

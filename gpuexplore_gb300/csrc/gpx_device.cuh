@@ -28,7 +28,11 @@ enum PorKind : uint32_t { POR_CAMPLE = 0, POR_AMPLE = 1, POR_STUBBORN = 2 };
 constexpr unsigned long long kMaxLaunches = 2ull * kMaxLevels; // exploration launches per run
 
 enum Mode : int { MODE_PLAIN = 0, MODE_POR = 1, MODE_PROVISO = 2 };
-enum Phase : uint32_t { PH_EXPAND = 0, PH_DECIDE = 1 };
+// A level's phases: the cycle proviso's lookup pass (DECIDE), the expansion
+// with inserts (EXPAND), and -- only when some insert found its whole probe
+// sequence full -- the placement of those keys with eviction (PLACE).
+enum Phase : uint32_t { PH_EXPAND = 0, PH_DECIDE = 1, PH_PLACE = 2 };
+constexpr int kEvictDepth = 4; // displacements one placement may chain
 
 // Control block shared by all blocks of the persistent kernel.
 // Run control block.  Fields that many warps touch during a level sit on
@@ -53,6 +57,10 @@ struct alignas(128) Ctrl {
     unsigned long long overflow_count; // keys whose probe sequence was full during this level
     unsigned long long evictions;      // keys displaced to make room
     unsigned long long launches;       // exploration launches of a graph-driven run
+    unsigned long long overflowed;     // keys that went through a placement phase (whole run)
+    unsigned long long place_ns;       // device time of the placement phases (whole run)
+    unsigned long long place_t0;       // start of the current placement phase
+    unsigned int place_blocks;         // blocks of place_kernel that have finished
     alignas(128) unsigned long long cursor;      // dynamic claims: offset beyond the static first claims
     alignas(128) unsigned long long store_count; // states appended to the store
     alignas(128) unsigned int bar_count;         // grid barrier arrivals
@@ -79,9 +87,13 @@ struct Params {
     uint32_t levels_per_launch;
     uint32_t total_warps;
     uint32_t por_kind;      // POR_CAMPLE, POR_AMPLE or POR_STUBBORN
-    // keys whose probe sequence was full, placed by the closing thread
+    // keys whose probe sequence was full, placed with eviction in a phase of their own
     void *overflow;
     unsigned long long overflow_cap;
+    // 128-bit claim entries {epoch, overflow index} deduplicating the overflow list
+    // ([0] holds the epoch counter, which survives runs); null: placement by one warp
+    unsigned long long *claim;
+    unsigned long long claim_cap; // entries, a power of two
     // learned cluster proposal (por == 2) and candidate logging (decide pass)
     const gpx_por_model *por_model;
     uint32_t learned;
@@ -110,6 +122,8 @@ static __device__ __forceinline__ uint64_t globaltimer() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
+
+static __device__ __forceinline__ void set_error(Ctrl *c, unsigned int code) { atomicCAS(&c->error, 0u, code); }
 
 static __device__ __forceinline__ void prefetch_l2(const void *p) {
     asm volatile("prefetch.global.L2 [%0];" : : "l"(p));
@@ -344,8 +358,8 @@ static __device__ __forceinline__ unsigned long long bucket_of(uint64_t h, int i
 
 // Find-or-insert.  Returns 0 if the key was present, 1 if this call inserted
 // it, 2 if every probed bucket was full.  Slots go from empty to a key exactly
-// once during a level (keys move only in place_evicting, when no other thread
-// inserts); every caller scans the same probe sequence and claims the first
+// once during a level (keys move only in the placement phase, when no other
+// thread inserts or looks up); every caller scans the same probe sequence and claims the first
 // empty slot it sees with a full-key CAS against the contents it read, so two
 // insertions of one key always meet in the same slot and exactly one wins.
 template <class K>
@@ -374,87 +388,202 @@ __device__ __forceinline__ int find_or_insert(K *table, unsigned long long nb, c
     return 2;
 }
 
-// Bounded eviction, run by a single thread while no other thread touches the
-// table (at the end of a level): place a key whose probe sequence was full by
-// moving one occupant V of that sequence to the first empty slot further along
-// V's own sequence, then writing the key where V was.  Both sequences keep
-// "every slot before a key's position is occupied", so lookups stay exact.
-// Returns 0 (already present), 1 (placed), 2 (no displacement found).
-template <class K>
-__device__ int place_evicting(K *table, unsigned long long nb, const K &key, unsigned long long seed,
-                              unsigned long long &evictions) {
-    constexpr int S = KT<K>::kSlots;
-    const uint64_t h = KT<K>::hash(key, seed);
-    const uint32_t tag = KT<K>::tag_of(key);
-    for (int i = 0; i < kMaxProbe; i++) { // placed meanwhile (a duplicate overflow entry) or room after all
-        K *b = table + bucket_of(h, i, nb) * S;
-        for (int j = 0; j < S; j++) {
-            K v = KT<K>::load(b + j);
-            if (KT<K>::eq(v, key)) return 0;
-            if (KT<K>::empty(v, tag)) {
-                b[j] = key;
-                return 1;
-            }
-        }
-    }
-    for (int i = 0; i < kMaxProbe; i++) {
-        const unsigned long long bi = bucket_of(h, i, nb);
-        K *b = table + bi * S;
-        for (int j = 0; j < S; j++) {
-            const K v = KT<K>::load(b + j);
-            const uint64_t hv = KT<K>::hash(v, seed);
-            int iv = -1;
-            for (int q = 0; q < kMaxProbe && iv < 0; q++)
-                if (bucket_of(hv, q, nb) == bi) iv = q;
-            for (int q = iv + 1; iv >= 0 && q < kMaxProbe; q++) {
-                K *bv = table + bucket_of(hv, q, nb) * S;
-                for (int jj = 0; jj < S; jj++) {
-                    if (KT<K>::empty(KT<K>::load(bv + jj), tag)) {
-                        bv[jj] = v;
-                        b[j] = key;
-                        evictions++;
-                        return 1;
-                    }
-                }
-            }
-        }
-    }
-    return 2;
+// ------------------------------------------------ placement with eviction
+//
+// A key whose 32 probe buckets were all full when it was inserted is appended to
+// an overflow list; when the level's inserts are done (no lookup or insert runs
+// any more) the list is placed.  A warp places one key X: its probe sequence is
+// scanned again (X may have been placed meanwhile by a duplicate entry, or a
+// slot freed, on the single-warp path); then, if the sequence is full, an
+// occupant W whose own sequence has a free slot after W's position is moved
+// there and X takes W's slot; if no occupant has one, an occupant is displaced
+// anyway and placed the same way in turn, for at most kEvictDepth moves.
+// Every move is a CAS from the contents just read, and a slot only ever changes
+// from free to a key or from one key to another, so every slot that was
+// occupied stays occupied: "every slot before a key's position is occupied"
+// holds throughout and lookups stay exact.  Moves go forward (W's slot is taken
+// before W is placed again), so no key is ever stored twice; a key that cannot
+// be placed within kEvictDepth moves is reported as GPX_ERR_TABLE_FULL.  Reads
+// are atomic (a 128-bit slot may change from one key to another while another
+// warp places its keys).
+
+template <class K> __device__ __forceinline__ K read_slot(K *p) {
+    if (sizeof(K) <= 8) return KT<K>::load(p);
+    const K z{};
+    return KT<K>::cas(p, z, z); // compares with zero, writes zero only over zero: an atomic read
 }
 
-// Place the level's overflowed keys (single thread, table quiescent); new ones
-// are appended to the store.  Sets GPX_ERR_TABLE_FULL when one cannot be placed.
-template <class K>
-__device__ void place_overflow(K *table, unsigned long long nb, K *store, uint32_t *label,
-                               unsigned long long store_cap, const K *overflow, unsigned long long overflow_cap,
-                               Ctrl *c, unsigned long long seed) {
-    unsigned long long n = c->overflow_count;
-    if (n > overflow_cap) {
-        n = overflow_cap;
-        atomicCAS(&c->error, 0u, (unsigned int)GPX_ERR_TABLE_FULL);
+template <class K> __device__ __forceinline__ K shfl_key(const K &k, int src) {
+    K o;
+    if constexpr (sizeof(K) == 4) {
+        o.v = __shfl_sync(kFull, k.v, src);
+    } else if constexpr (sizeof(K) == 8) {
+        o.v = __shfl_sync(kFull, k.v, src);
+    } else {
+        o.lo = __shfl_sync(kFull, k.lo, src);
+        o.hi = __shfl_sync(kFull, k.hi, src);
     }
-    unsigned long long ev = 0;
+    return o;
+}
+
+// Place warp-uniform key x with eviction (all 32 lanes call it; kMaxProbe == 32,
+// one probe bucket per lane).  Returns 0 if x was present, 1 if it was placed,
+// 2 if a key could not be placed.  `moves` counts displaced keys (lane 0).
+template <class K>
+__device__ int place_warp(K *table, unsigned long long nb, K x, unsigned long long seed, uint32_t lane,
+                          unsigned long long &moves) {
+    static_assert(kMaxProbe == 32, "one probe bucket per lane");
+    constexpr int S = KT<K>::kSlots;
+    int depth = 0; // keys displaced so far; x is the key now looking for a slot
+    for (int round = 0; round < 64; round++) { // each round returns, goes one move deeper or retries a lost race
+        const uint64_t hx = KT<K>::hash(x, seed);
+        const uint32_t tag = KT<K>::tag_of(x);
+        const unsigned long long bx = bucket_of(hx, (int)lane, nb);
+        K v[S];
+        bool has = false;
+        int fre = -1;
+#pragma unroll
+        for (int j = 0; j < S; j++) {
+            v[j] = read_slot<K>(table + bx * S + j);
+            if (KT<K>::eq(v[j], x)) has = true;
+            if (fre < 0 && KT<K>::empty(v[j], tag)) fre = j;
+        }
+        if (__any_sync(kFull, has)) return depth ? 1 : 0; // (a displaced key is never found: stored once)
+        const uint32_t fm = __ballot_sync(kFull, fre >= 0);
+        if (fm) { // the first free slot in probe order
+            const int L = __ffs(fm) - 1;
+            int ok = 0;
+            if ((int)lane == L) ok = KT<K>::eq(KT<K>::cas(table + bx * S + fre, v[fre], x), v[fre]);
+            if (__shfl_sync(kFull, ok, L)) return 1;
+            continue; // another placement took it: read again
+        }
+        if (depth >= kEvictDepth) return 2;
+        // Full sequence.  Occupants in probe order, one at a time, each checked by
+        // the whole warp for a free slot later in its own sequence.
+        int step = 0; // 1: x placed, its occupant w is next (one move deeper); 2: lost a race
+        for (int o = 0; o < 32 * S && !step; o++) {
+            const int ob = o / S, oj = o % S;
+            const unsigned long long bo = __shfl_sync(kFull, bx, ob);
+            K w = v[0];
+#pragma unroll
+            for (int j = 0; j < S; j++) {
+                const K t = shfl_key<K>(v[j], ob);
+                if (j == oj) w = t;
+            }
+            const unsigned long long bw = bucket_of(KT<K>::hash(w, seed), (int)lane, nb);
+            const uint32_t at = __ballot_sync(kFull, bw == bo); // w sits at its first visit of bo
+            if (!at) continue;
+            const int iw = __ffs(at) - 1;
+            int fw = -1;
+            K u[S];
+#pragma unroll
+            for (int j = 0; j < S; j++) u[j] = K{};
+            if ((int)lane > iw) {
+#pragma unroll
+                for (int j = 0; j < S; j++) {
+                    u[j] = read_slot<K>(table + bw * S + j);
+                    if (fw < 0 && KT<K>::empty(u[j], tag)) fw = j;
+                }
+            }
+            const uint32_t wm = __ballot_sync(kFull, fw >= 0);
+            if (!wm) continue;
+            // x takes w's slot first, then w the free slot: never two copies of w
+            int ok = 0;
+            if ((int)lane == ob) ok = KT<K>::eq(KT<K>::cas(table + bo * S + oj, w, x), w);
+            if (!__shfl_sync(kFull, ok, ob)) {
+                step = 2;
+                break;
+            }
+            if (lane == 0) moves++;
+            const int L = __ffs(wm) - 1;
+            int ok2 = 0;
+            if ((int)lane == L) ok2 = KT<K>::eq(KT<K>::cas(table + bw * S + fw, u[fw], w), u[fw]);
+            if (__shfl_sync(kFull, ok2, L)) return 1;
+            x = w; // lost the free slot: place w next
+            depth++;
+            step = 1;
+        }
+        if (step) continue;
+        // No occupant has a free slot later in its sequence: displace a seeded one
+        // anyway and place it next.
+        const int o = (int)(mix64(hx + (uint64_t)depth) % (uint64_t)(32 * S));
+        const int ob = o / S, oj = o % S;
+        const unsigned long long bo = __shfl_sync(kFull, bx, ob);
+        K w = v[0];
+#pragma unroll
+        for (int j = 0; j < S; j++) {
+            const K t = shfl_key<K>(v[j], ob);
+            if (j == oj) w = t;
+        }
+        int ok = 0;
+        if ((int)lane == ob) ok = KT<K>::eq(KT<K>::cas(table + bo * S + oj, w, x), w);
+        if (__shfl_sync(kFull, ok, ob)) {
+            if (lane == 0) moves++;
+            x = w;
+            depth++;
+        }
+    }
+    return 2; // kept losing races (bounded: the run reports a full table)
+}
+
+// Place the overflow list of a quiescent table with one warp, entry by entry
+// (a later duplicate of a key finds it placed); new keys are appended to the
+// store.  Used where a single warp closes a level (the many-network kernel).
+template <class K>
+__device__ void place_list_warp(K *table, unsigned long long nb, K *store, uint32_t *label,
+                                unsigned long long store_cap, const K *overflow, unsigned long long n, Ctrl *c,
+                                unsigned long long seed, uint32_t lane) {
+    unsigned long long moves = 0, placed = 0;
     for (unsigned long long k = 0; k < n; k++) {
-        const K key = KT<K>::load(overflow + k);
-        int r = place_evicting<K>(table, nb, key, seed, ev);
+        const K x = KT<K>::load(overflow + k);
+        const int r = place_warp<K>(table, nb, x, seed, lane, moves);
         if (r == 2) {
-            atomicCAS(&c->error, 0u, (unsigned int)GPX_ERR_TABLE_FULL);
+            if (lane == 0) set_error(c, GPX_ERR_TABLE_FULL);
             break;
         }
-        if (r == 1) {
-            unsigned long long idx = c->store_count++;
+        if (r == 1 && lane == 0) {
+            const unsigned long long idx = c->store_count++;
             if (idx < store_cap) {
-                store[idx] = key;
+                store[idx] = x;
                 if (label) label[idx] = 0; // its inserting move is not kept: nothing is pruned from it
             } else {
-                atomicCAS(&c->error, 0u, (unsigned int)GPX_ERR_STORE_FULL);
+                set_error(c, GPX_ERR_STORE_FULL);
             }
-            c->inserts++;
+            placed++;
         }
     }
-    c->evictions += ev;
-    c->overflow_count = 0;
-    __threadfence();
+    if (lane == 0) {
+        atomicAdd(&c->inserts, placed);
+        atomicAdd(&c->evictions, moves);
+        atomicAdd(&c->overflowed, n);
+    }
+    __syncwarp();
+}
+
+// The first overflow entry of key x (index k) wins a claim; a later entry of the
+// same key (two threads inserted one new state while its sequence was full)
+// finds the claim and is skipped, so each distinct key is placed once.
+// Entries are {epoch, index} pairs; an entry of an older epoch is free.
+template <class K>
+__device__ bool claim_overflow(unsigned long long *claim, unsigned long long cap, unsigned long long epoch,
+                               const K *overflow, unsigned long long k, const K &x, uint64_t h) {
+    const unsigned long long mask = cap - 1;
+    for (unsigned long long i = 0; i < cap; i++) {
+        const unsigned long long pos = 2 + 2 * ((h + i) & mask); // [0, 2): the epoch counter
+        unsigned long long olo, ohi;
+        cas128(claim + pos, 0ull, 0ull, 0ull, 0ull, olo, ohi); // atomic read
+        for (int tries = 0; tries < 64; tries++) {
+            if (olo == epoch) break;
+            unsigned long long nlo, nhi;
+            cas128(claim + pos, olo, ohi, epoch, k, nlo, nhi);
+            if (nlo == olo && nhi == ohi) return true; // claimed
+            olo = nlo;
+            ohi = nhi;
+        }
+        if (olo != epoch) return true; // unreachable in practice: behave as the first entry
+        if (KT<K>::eq(KT<K>::load(overflow + ohi), x)) return ohi == k;
+    }
+    return true;
 }
 
 // Lookup in a table no one writes to during the call (the decide pass of the
@@ -563,8 +692,6 @@ struct MView {
         return rec_of(d, s);
     }
 };
-
-static __device__ __forceinline__ void set_error(Ctrl *c, unsigned int code) { atomicCAS(&c->error, 0u, code); }
 
 static __device__ __forceinline__ unsigned int vload(const unsigned int *p) { return *(volatile const unsigned int *)p; }
 static __device__ __forceinline__ unsigned long long vload(const unsigned long long *p) {

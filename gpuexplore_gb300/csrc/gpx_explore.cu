@@ -63,9 +63,28 @@ template <class K, int MODE> __device__ void close_phase(const Params &P) {
         c->cursor = 0;
         return;
     }
-    if (c->overflow_count)
-        place_overflow<K>((K *)P.table, P.nbuckets, (K *)P.store, P.label, P.store_cap, (const K *)P.overflow,
-                          P.overflow_cap, c, P.seed);
+    if (c->phase == PH_PLACE) { // the overflowed keys of this level are placed
+        c->place_ns += globaltimer() - c->place_t0;
+        c->overflow_count = 0;
+    } else if (c->overflow_count) {
+        if (c->overflow_count <= P.overflow_cap && !c->error) {
+            // The level's inserts are done.  The exploration kernel returns and
+            // place_kernel places the overflowed keys with every warp (PH_PLACE),
+            // then closes the level; the relaunch continues with the next one.
+            // (A phase of the persistent kernel would cost its hot loop
+            // registers: the placement code stays out of it.)
+            c->phase = PH_PLACE;
+            c->cursor = 0;
+            c->place_t0 = globaltimer();
+            c->overflowed += c->overflow_count;
+            c->place_blocks = 0;
+            if (P.claim) P.claim[0]++; // a new claim epoch (the counter survives runs)
+            c->pause = 1;
+            return;
+        }
+        set_error(c, GPX_ERR_TABLE_FULL); // more keys than the overflow list holds
+        c->overflow_count = 0;
+    }
     unsigned long long hi = c->hi;
     unsigned long long newhi = c->store_count;
     if (newhi > P.store_cap) newhi = P.store_cap;
@@ -141,6 +160,55 @@ template <class K, int MODE> __device__ void grid_barrier(const Params &P, Level
         read_view(c, view);
     }
     __syncthreads();
+}
+
+// The placement phase (PH_PLACE), run after a level whose inserts left keys in
+// the overflow list: warp gw places entries gw, gw + warps, ... (the table is
+// quiescent: the exploration kernel has returned).  A claim table lets only the
+// first entry of each distinct key place it.  The last block to finish closes
+// the level.  Launched after every exploration launch; it returns at once
+// unless the level is waiting for placement.
+template <class K, int MODE> __global__ void __launch_bounds__(256) place_kernel(Params P) {
+    Ctrl *c = P.ctrl;
+    if (vload(&c->phase) != PH_PLACE || vload(&c->error)) return;
+    const uint32_t lane = threadIdx.x & 31;
+    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    const unsigned long long gw = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const unsigned long long n = vload(&c->overflow_count);
+    const unsigned long long epoch = P.claim ? vload(P.claim) : 0;
+    K *table = (K *)P.table;
+    unsigned long long moves = 0, inserts = 0;
+    for (unsigned long long k = gw; k < n && k < P.overflow_cap; k += warps) {
+        const K x = KT<K>::load((const K *)P.overflow + k);
+        int mine = 1;
+        if (P.claim && lane == 0)
+            mine = claim_overflow<K>(P.claim, P.claim_cap, epoch, (const K *)P.overflow, k, x,
+                                     KT<K>::hash(x, P.seed ^ 0xC1A1Full));
+        if (!__shfl_sync(kFull, mine, 0)) continue; // a later entry of a key already claimed
+        const int r = place_warp<K>(table, P.nbuckets, x, P.seed, lane, moves);
+        if (r == 2) {
+            if (lane == 0) set_error(c, GPX_ERR_TABLE_FULL);
+        } else if (r == 1 && lane == 0) { // a new state: the store records it for the next level
+            const unsigned long long idx = atomicAdd(&c->store_count, 1ull);
+            if (idx < P.store_cap) {
+                ((K *)P.store)[idx] = x;
+                if (P.label) P.label[idx] = 0; // its inserting move is not kept: nothing is pruned from it
+            } else {
+                set_error(c, GPX_ERR_STORE_FULL);
+            }
+            inserts++;
+        }
+    }
+    if (lane == 0 && moves) atomicAdd(&c->evictions, moves);
+    if (lane == 0 && inserts) atomicAdd(&c->inserts, inserts);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&c->place_blocks, 1u) == gridDim.x - 1) { // the last block: every key is placed
+            __threadfence();
+            close_phase<K, MODE>(P);
+        }
+    }
 }
 
 template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_kernel(Params P) {
@@ -332,6 +400,7 @@ const char *kStatusStrings[] = {"ok",
 
 struct KernelSet {
     void (*explore[3])(Params);
+    void (*place[3])(Params);
     void (*init)(Params, unsigned int, unsigned int);
     void (*set_hash)(cudaStream_t, int blocks, const void *store, unsigned long long count,
                      const unsigned long long *count_dev, unsigned long long cap, uint32_t words,
@@ -362,6 +431,9 @@ template <class K> KernelSet kernels_for() {
     s.explore[0] = explore_kernel<K, MODE_PLAIN>;
     s.explore[1] = explore_kernel<K, MODE_POR>;
     s.explore[2] = explore_kernel<K, MODE_PROVISO>;
+    s.place[0] = place_kernel<K, MODE_PLAIN>;
+    s.place[1] = place_kernel<K, MODE_POR>;
+    s.place[2] = place_kernel<K, MODE_PROVISO>;
     s.init = init_kernel<K>;
     s.scratch_bytes[0] = sizeof(WarpScratch<K, MODE_PLAIN>);
     s.scratch_bytes[1] = sizeof(WarpScratch<K, MODE_POR>);
@@ -386,6 +458,8 @@ template <class K> KernelSet kernels_for() {
 struct GraphKey {
     Params P;
     void (*kern)(Params);
+    void (*place)(Params);
+    int place_blocks;
     int blocks, threads;
     size_t smem;
     unsigned int first_phase;
@@ -393,6 +467,7 @@ struct GraphKey {
     int collect;
     void *log_count;
     int clear; // the run zeroes the table first
+    int set_hash; // the run ends with the set-hash pass
 };
 constexpr uint32_t kGraphLevels = 4096; // level counts read back by the graph itself
 
@@ -417,6 +492,8 @@ struct gpx_explorer {
     uint32_t *d_label = nullptr; // plain mode with prune_commuting: inserting move per store position
     void *d_overflow = nullptr; // keys whose probe sequence was full during a level
     unsigned long long overflow_cap = 0;
+    unsigned long long *d_claim = nullptr; // claim table of the placement phase (epoch counter + entries)
+    unsigned long long claim_cap = 0;
     unsigned long long *d_levels = nullptr;
     unsigned long long *d_scalar = nullptr;
     Ctrl *d_ctrl = nullptr;
@@ -451,6 +528,19 @@ namespace {
 
 // gpx_options.por: 1 cample, 2 cample with the learned proposal, 3 ample, 4 stubborn
 uint32_t por_kind_of(int por) { return por == 3 ? POR_AMPLE : (por == 4 ? POR_STUBBORN : POR_CAMPLE); }
+
+// Checks every entry point that takes gpx_options makes before it touches the
+// device, so that the same options are accepted or refused everywhere.  Sizes
+// are bounded so that no byte count derived from them overflows 64 bits.
+int check_options(const gpx_options *o) {
+    if (!o || o->struct_size != sizeof(gpx_options)) return GPX_ERR_INVALID;
+    if (o->bucket_bytes != 0 && o->bucket_bytes != 32) return GPX_ERR_INVALID;
+    if (o->por < 0 || o->por > 4) return GPX_ERR_INVALID;
+    if (o->property < GPX_PROP_NONE || o->property > GPX_PROP_LIVENESS) return GPX_ERR_INVALID;
+    if (o->threads < 0 || o->threads % 32 || o->threads > 256) return GPX_ERR_INVALID;
+    if (o->q_words > (1ull << 60) || o->store_states > (1ull << 58)) return GPX_ERR_INVALID;
+    return GPX_OK;
+}
 
 // Slot form for a state width.  A table the explorer keeps across runs takes
 // the generation-tagged form when the state fits its 112 bits.
@@ -537,6 +627,8 @@ Params make_params(gpx_explorer *ex) {
     P.label = ex->mode == MODE_PLAIN ? ex->d_label : nullptr;
     P.overflow = ex->d_overflow;
     P.overflow_cap = ex->overflow_cap;
+    P.claim = ex->d_claim;
+    P.claim_cap = ex->claim_cap;
     P.levels = ex->d_levels;
     P.ctrl = ex->d_ctrl;
     P.seed = ex->o.seed;
@@ -558,6 +650,9 @@ Params make_params(gpx_explorer *ex) {
     return P;
 }
 
+// Grid of place_kernel: a few blocks per SM (most launches return at once).
+int place_grid(const gpx_explorer *ex) { return 4 * ex->prop.multiProcessorCount; }
+
 int count_blocks(const gpx_explorer *ex) {
     return (int)std::max<unsigned long long>(1, std::min<unsigned long long>((ex->slots + 255) / 256, 8192));
 }
@@ -576,6 +671,8 @@ GraphKey graph_key(const gpx_explorer *ex, const Params &P, unsigned int first_p
     memset(&k, 0, sizeof k);
     k.P = P;
     k.kern = ex->ks.explore[ex->mode];
+    k.place = ex->ks.place[ex->mode];
+    k.place_blocks = place_grid(ex);
     k.blocks = ex->blocks;
     k.threads = ex->threads;
     k.smem = ex->smem;
@@ -584,11 +681,13 @@ GraphKey graph_key(const gpx_explorer *ex, const Params &P, unsigned int first_p
     k.collect = (ex->o.collect_states || ex->o.verbosity >= 2) ? 1 : 0;
     k.log_count = ex->d_log_count;
     k.clear = clear ? 1 : 0;
+    k.set_hash = ex->o.set_hash ? 1 : 0;
     return k;
 }
 
 // Record one run into a graph on ex->st:
-//   [zero the table] + init -> while (more) { exploration launch; relaunch_kernel } -> set hash -> read-back
+//   [zero the table] + init -> while (more) { exploration launch; placement; relaunch_kernel }
+//   -> [set hash] -> read-back
 // The loop's condition is set on the device by relaunch_kernel, so a -k run
 // needs no host round trip between launches.
 cudaError_t capture_run(gpx_explorer *ex, const GraphKey &k, cudaGraph_t *out) {
@@ -629,6 +728,7 @@ cudaError_t capture_run(gpx_explorer *ex, const GraphKey &k, cudaGraph_t *out) {
         body_open = true;
         void *args[] = {&P};
         GPX_CAP(cudaLaunchCooperativeKernel((const void *)k.kern, dim3(k.blocks), dim3(k.threads), args, k.smem, sb));
+        k.place<<<k.place_blocks, 256, 0, sb>>>(P); // returns at once unless a level waits for placement
         relaunch_kernel<<<1, 1, 0, sb>>>(ex->d_ctrl, loop);
         GPX_CAP(cudaGetLastError());
         cudaGraph_t body = nullptr; // owned by the conditional node
@@ -637,8 +737,12 @@ cudaError_t capture_run(gpx_explorer *ex, const GraphKey &k, cudaGraph_t *out) {
 
         GPX_CAP(cudaEventRecordWithFlags(ex->ev[3], st, cudaEventRecordExternal));
         GPX_CAP(cudaMemsetAsync(ex->d_scalar, 0, 16, st));
-        int hb = (int)std::max<unsigned long long>(1, std::min<unsigned long long>((ex->store_cap + 255) / 256, 4096));
-        ex->ks.set_hash(st, hb, ex->d_store, 0, &ex->d_ctrl->store_count, ex->store_cap, k.key_words, ex->d_scalar);
+        if (k.set_hash) {
+            int hb = (int)std::max<unsigned long long>(1, std::min<unsigned long long>((ex->store_cap + 255) / 256,
+                                                                                      4096));
+            ex->ks.set_hash(st, hb, ex->d_store, 0, &ex->d_ctrl->store_count, ex->store_cap, k.key_words,
+                            ex->d_scalar);
+        }
         if (k.collect) ex->ks.count(st, count_blocks(ex), ex->d_table, ex->slots, ex->d_ctrl, ex->d_scalar + 1);
         GPX_CAP(cudaGetLastError());
         GPX_CAP(cudaMemcpyAsync(ex->h_ctrl, ex->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));
@@ -840,6 +944,7 @@ void gpx_explorer_destroy(gpx_explorer *ex) {
     if (ex->d_sel) cudaFree(ex->d_sel);
     if (ex->d_label) cudaFree(ex->d_label);
     if (ex->d_overflow) cudaFree(ex->d_overflow);
+    if (ex->d_claim) cudaFree(ex->d_claim);
     if (ex->d_levels) cudaFree(ex->d_levels);
     if (ex->d_scalar) cudaFree(ex->d_scalar);
     if (ex->d_ctrl) cudaFree(ex->d_ctrl);
@@ -854,9 +959,8 @@ void gpx_explorer_destroy(gpx_explorer *ex) {
 }
 
 int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_explorer **out) {
-    if (!model || !opts || !out || opts->struct_size != sizeof(gpx_options)) return GPX_ERR_INVALID;
-    if (opts->bucket_bytes != 0 && opts->bucket_bytes != 32) return GPX_ERR_INVALID;
-    if (opts->por < 0 || opts->por > 4) return GPX_ERR_INVALID;
+    if (!model || !out) return GPX_ERR_INVALID;
+    if (int bad = check_options(opts)) return bad;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPX_ERR_NO_GPU;
     if (opts->device < 0 || opts->device >= ndev) return GPX_ERR_INVALID;
@@ -900,7 +1004,11 @@ int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_exp
     unsigned long long cap = opts->store_states ? opts->store_states : ex->slots;
     size_t margin = (size_t)512 << 20;
     size_t avail = free_b > tb + margin ? free_b - tb - margin : 0;
-    if (!opts->store_states && cap * per_state > avail) cap = avail / per_state;
+    // compare in states, not bytes: cap * per_state could wrap for an explicit store_states
+    if (cap > avail / per_state) {
+        if (opts->store_states) return fail(GPX_ERR_NOMEM);
+        cap = avail / per_state;
+    }
     if (cap < 1) return fail(GPX_ERR_NOMEM);
     ex->store_cap = cap;
     if (cudaMalloc(&ex->d_table, tb) != cudaSuccess) return fail(GPX_ERR_NOMEM);
@@ -909,6 +1017,9 @@ int gpx_explorer_create(const gpx_model *model, const gpx_options *opts, gpx_exp
     if (labels && cudaMalloc(&ex->d_label, cap * 4) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     ex->overflow_cap = 1u << 16;
     if (cudaMalloc(&ex->d_overflow, ex->overflow_cap * ex->ks.slot_bytes) != cudaSuccess) return fail(GPX_ERR_NOMEM);
+    ex->claim_cap = 2 * ex->overflow_cap; // entries of 16 bytes after a 16-byte epoch counter
+    if (cudaMalloc(&ex->d_claim, (2 + 2 * ex->claim_cap) * 8) != cudaSuccess) return fail(GPX_ERR_NOMEM);
+    if (cudaMemset(ex->d_claim, 0, (2 + 2 * ex->claim_cap) * 8) != cudaSuccess) return fail(GPX_ERR_CUDA);
     if (cudaMalloc(&ex->d_levels, (size_t)kMaxLevels * 8) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (cudaMalloc(&ex->d_scalar, 64) != cudaSuccess) return fail(GPX_ERR_NOMEM);
     if (cudaMalloc(&ex->d_ctrl, sizeof(Ctrl)) != cudaSuccess) return fail(GPX_ERR_NOMEM);
@@ -991,6 +1102,8 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
             GPX_CUDA(cudaEventRecord(ex->ev[2], ex->st));
             GPX_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(ex->blocks), dim3(ex->threads), args,
                                                  ex->smem, ex->st));
+            ex->ks.place[ex->mode]<<<place_grid(ex), 256, 0, ex->st>>>(P); // a level waiting for placement
+            GPX_CUDA(cudaGetLastError());
             GPX_CUDA(cudaEventRecord(ex->ev[3], ex->st));
             launches++;
             GPX_CUDA(cudaMemcpyAsync(ex->h_ctrl, ex->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, ex->st));
@@ -1039,6 +1152,8 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     r->inserts = c.inserts;
     r->evictions = c.evictions;
     r->pruned = c.pruned;
+    r->overflowed = c.overflowed;
+    r->evict_ms = c.place_ns * 1e-6;
     r->expanded = c.expanded;
     r->launches = launches;
     r->kernel_ms = kernel_ms;
@@ -1065,10 +1180,11 @@ int gpx_explorer_run(gpx_explorer *ex, gpx_result *r) {
     } else {
         GPX_CUDA(cudaMemcpyAsync(r->level_counts, ex->d_levels, sizeof(uint64_t) * c.nlevels, cudaMemcpyDeviceToHost,
                                  ex->st));
-        // set hash over the visited states
+        // set hash over the visited states (gpx_options.set_hash)
         GPX_CUDA(cudaMemsetAsync(ex->d_scalar, 0, 16, ex->st));
         int blocks = (int)std::min<unsigned long long>((count + 255) / 256, 4096);
-        ex->ks.set_hash(ex->st, std::max(blocks, 1), ex->d_store, count, nullptr, 0, r->key_words, ex->d_scalar);
+        if (ex->o.set_hash)
+            ex->ks.set_hash(ex->st, std::max(blocks, 1), ex->d_store, count, nullptr, 0, r->key_words, ex->d_scalar);
         if (ex->o.collect_states || ex->o.verbosity >= 2)
             ex->ks.count(ex->st, count_blocks(ex), ex->d_table, ex->slots, ex->d_ctrl, ex->d_scalar + 1);
         GPX_CUDA(cudaGetLastError());
@@ -1326,10 +1442,11 @@ extern "C" int gpx_random_gather_probe(int device, uint64_t bytes, double *gathe
 // device scratch -- control block, set-hash scalars, level counts, model,
 // hash table, state store, cluster array -- carved out of one static device
 // array, so the call allocates nothing.  Layout (byte offsets):
-//   [0, 256)            Ctrl
-//   [256, 320)          set-hash / table-count scalars
+//   [0, 1024)           Ctrl (at most 1024 bytes, checked at compile time)
+//   [1024, 1088)        set-hash / table-count scalars
 //   [4096, +8 MiB)      level counts (kMaxLevels entries)
-//   then                model words, hash table, state store, cluster array
+//   then                model words, hash table, state store, cluster array,
+//                       each on a 256-byte boundary
 static __device__ __align__(256) unsigned char g_gpx_noalloc_scratch[GPX_NOALLOC_SCRATCH_BYTES];
 
 namespace {
@@ -1361,7 +1478,8 @@ size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *opts, uint64_t *level_counts,
                                    uint32_t level_capacity, gpx_result *r) {
-    if (!model || !opts || !r || opts->struct_size != sizeof(gpx_options)) return GPX_ERR_INVALID;
+    if (!model || !r) return GPX_ERR_INVALID;
+    if (int bad = check_options(opts)) return bad;
     if (!level_counts && level_capacity) return GPX_ERR_INVALID;
     memset(r, 0, sizeof *r);
     r->struct_size = sizeof *r;
@@ -1396,11 +1514,13 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     const size_t bucket_bytes = (size_t)ks.slot_bytes * ks.bucket_slots;
     const size_t per_state = ks.slot_bytes + (mode == MODE_PROVISO ? 4 : 0);
     size_t left = total - off_table;
-    size_t tb = opts->q_words ? (size_t)opts->q_words * 4 : left / 2;
+    size_t tb = opts->q_words ? (size_t)opts->q_words * 4 : left / 2; // q_words <= 2^60: no wrap
     tb = tb / (2 * bucket_bytes) * (2 * bucket_bytes);
-    // the store and the cluster array each start on a 256-byte boundary
-    size_t cap = opts->store_states ? (size_t)opts->store_states : (left > tb + 512 ? (left - tb - 512) / per_state : 0);
-    if (tb < 2 * bucket_bytes || cap < 1 || tb + cap * per_state + 512 > left) {
+    // the store and the cluster array each start on a 256-byte boundary (512 bytes of slack);
+    // sizes are compared in states so that a huge store_states cannot wrap the product
+    const size_t max_cap = (tb <= left && left - tb > 512) ? (left - tb - 512) / per_state : 0;
+    size_t cap = opts->store_states ? (size_t)opts->store_states : max_cap;
+    if (tb < 2 * bucket_bytes || tb > left || cap < 1 || cap > max_cap) {
         fprintf(stderr,
                 "gpx_explore_noalloc: requested %zu table bytes + %zu states x %zu bytes, but only %zu bytes of the "
                 "%zu-byte scratch array are left after the control block, level counts and model\n",
@@ -1418,7 +1538,6 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     cudaDeviceProp prop;
     GPX_CUDA(cudaGetDeviceProperties(&prop, opts->device));
     int threads = opts->threads > 0 ? opts->threads : 256;
-    if (threads % 32 || threads > 256) return GPX_ERR_INVALID;
     size_t scratch = (size_t)(threads / 32) * ks.scratch_bytes[mode];
     size_t mb = (model_bytes + 127) & ~(size_t)127;
     bool in_smem = (mb + scratch <= prop.sharedMemPerBlockOptin) && model_bytes <= 96 * 1024;
@@ -1455,8 +1574,9 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     P.por_kind = por_kind_of(opts->por);
 
     // clear what must start at zero (the array keeps the previous call's contents;
-    // init_kernel resets the control block)
-    cudaStream_t st = 0;
+    // init_kernel resets the control block).  The calling thread's per-thread
+    // default stream: no implicit wait on the caller's other blocking streams.
+    cudaStream_t st = cudaStreamPerThread;
     Ctrl c;
     GPX_CUDA(cudaMemcpyAsync(base + off_model, model->dec.words.data(), model_bytes, cudaMemcpyHostToDevice, st));
     GPX_CUDA(cudaMemsetAsync(P.table, 0, tb, st));
@@ -1481,7 +1601,7 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     auto t_end = std::chrono::steady_clock::now();
     unsigned long long count = std::min<unsigned long long>(c.store_count, cap);
     int hb = (int)std::max<unsigned long long>(1, std::min<unsigned long long>((count + 255) / 256, 4096));
-    ks.set_hash(st, hb, P.store, count, nullptr, 0, model->dec.key_words, d_scalar);
+    if (opts->set_hash) ks.set_hash(st, hb, P.store, count, nullptr, 0, model->dec.key_words, d_scalar);
     GPX_CUDA(cudaGetLastError());
     unsigned long long h = 0;
     GPX_CUDA(cudaMemcpyAsync(&h, d_scalar, sizeof h, cudaMemcpyDeviceToHost, st));

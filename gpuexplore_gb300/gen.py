@@ -2,11 +2,13 @@
 set are not available, so the benchmark and test networks are built here).
 
 Every generator is a pure function of its seed (Python's `random.Random`, so the
-same file is produced on any host).  The generated networks keep to the subset
-of the gpf semantics on which the reference's two successor kernels agree
-(GPUexplore.cu:756-1189 vs 1191-1733): every synchronisation rule has at least
-two participants, one (process, state, action) never needs more than two
+same file is produced on any host).  The generated networks keep by default to
+the subset of the gpf semantics on which the reference's two successor kernels
+agree (GPUexplore.cu:756-1189 vs 1191-1733): every synchronisation rule has at
+least two participants, one (process, state, action) never needs more than two
 transition entries (max_buf_ints <= 2), and targets are never repeated.
+:func:`corner_network` (with gpf.encode's max_slots / repeat_seed) leaves that
+subset on purpose.
 
 Families
 --------
@@ -18,6 +20,8 @@ random_network  n processes with U[lo, hi] states, out-degree U[1, 4], a share o
 clustered       processes in seeded clusters, transitions mostly inside the
                 cluster (tau or intra-cluster sync) and a share of
                 cross-cluster synchronisations
+corner_network  random networks with single-party synchronisation rules and
+                few actions per process (many targets per action)
 batch           many random networks of uneven sizes
 """
 from __future__ import annotations
@@ -230,12 +234,20 @@ def progress_network(seed: int, nprocs: int = 5, states: Tuple[int, int] = (3, 6
 
 def _sync_pool(rng: random.Random, procs: List[int], nactions: int,
                parties: Tuple[int, int], groups: Optional[List[List[int]]] = None,
-               p_subrule: float = 0.25) -> Tuple[Dict[int, List[int]], List[List[int]]]:
-    """Create `nactions` synchronising actions over `procs`; return (rules, per-process action lists)."""
+               p_subrule: float = 0.25, single: float = 0.0) -> Tuple[Dict[int, List[int]], List[List[int]]]:
+    """Create `nactions` synchronising actions over `procs`; return (rules, per-process action lists).
+    With `single` > 0 an action is, with that probability, a one-party rule of
+    a seeded process, and a multi-party action gets, with that probability, a
+    one-party rule of one member beside its full rule."""
     rules: Dict[int, List[int]] = {}
     acts_of: Dict[int, List[int]] = {p: [] for p in procs}
     for a in range(nactions):
         pool = procs if groups is None else rng.choice(groups)
+        if single and rng.random() < single:
+            p = rng.choice(pool)
+            rules[a] = [1 << p]
+            acts_of[p].append(a)
+            continue
         k = min(len(pool), rng.randint(parties[0], parties[1]))
         if k < 2:
             continue
@@ -247,6 +259,8 @@ def _sync_pool(rng: random.Random, procs: List[int], nactions: int,
         if k >= 3 and rng.random() < p_subrule:
             sub = sorted(rng.sample(members, 2))
             rs.append((1 << sub[0]) | (1 << sub[1]))
+        if single and rng.random() < single:
+            rs.append(1 << rng.choice(members))
         rules[a] = rs
         for p in members:
             acts_of[p].append(a)
@@ -256,12 +270,14 @@ def _sync_pool(rng: random.Random, procs: List[int], nactions: int,
 def random_network(seed: int, nprocs: int = 16, states: Tuple[int, int] = (8, 32),
                    outdeg: Tuple[int, int] = (1, 4), sync_frac: float = 0.2,
                    parties: Tuple[int, int] = (2, 3), safety: bool = True,
-                   nactions: Optional[int] = None, nstates: Optional[List[int]] = None) -> Network:
+                   nactions: Optional[int] = None, nstates: Optional[List[int]] = None,
+                   single: float = 0.0) -> Network:
     """Random network: `nprocs` processes with U[states] local states (or exactly
     `nstates`), out-degree U[outdeg] per state, each transition synchronising with
     probability `sync_frac` (an action shared by 2-3 seeded processes), otherwise
     local.  With `safety`, a monitor over a seeded pair of error local states is
-    appended (see :func:`add_safety_monitor`), giving nprocs+1 processes."""
+    appended (see :func:`add_safety_monitor`), giving nprocs+1 processes.
+    `single` adds one-party synchronisation rules (see :func:`_sync_pool`)."""
     rng = random.Random(seed)
     nst = [rng.randint(states[0], states[1]) for _ in range(nprocs)]
     if nstates is not None:
@@ -269,7 +285,7 @@ def random_network(seed: int, nprocs: int = 16, states: Tuple[int, int] = (8, 32
         nprocs = len(nst)
     net = _empty(nst)
     na = nactions if nactions is not None else 2 * nprocs
-    rules, acts_of = _sync_pool(rng, list(range(nprocs)), na, parties)
+    rules, acts_of = _sync_pool(rng, list(range(nprocs)), na, parties, single=single)
     net.rules = rules
     err = None
     if safety:
@@ -289,6 +305,19 @@ def random_network(seed: int, nprocs: int = 16, states: Tuple[int, int] = (8, 32
         (i, a), (j, b) = sorted(err.items())
         net = add_safety_monitor(net, i, a, j, b)
     return net
+
+
+def corner_network(seed: int, nprocs: int = 8, states: Tuple[int, int] = (3, 6),
+                   outdeg: Tuple[int, int] = (2, 5), sync_frac: float = 0.6, single: float = 0.3,
+                   safety: bool = True) -> Network:
+    """A random network outside the subset both reference kernels agree on:
+    single-party synchronisation rules (alone, or beside a multi-party rule of
+    the same action), and only about one action per process, so a state often
+    has three or more targets for one action.  Encoded with gpf.encode's
+    max_slots=1 those targets take one entry each (max_buf_ints >= 3, entries
+    with empty slots); repeat_seed repeats targets."""
+    return random_network(seed, nprocs=nprocs, states=states, outdeg=outdeg, sync_frac=sync_frac,
+                          nactions=nprocs, single=single, safety=safety)
 
 
 def clustered(seed: int, nprocs: int = 24, nclusters: Tuple[int, int] = (4, 6),

@@ -39,8 +39,9 @@ state 1 is the error state (GPUexplore.cu:927-935, 1063-1069).
 """
 from __future__ import annotations
 
+import random
 from dataclasses import dataclass, field
-from typing import Dict, List, Sequence
+from typing import Dict, List, Optional, Sequence
 
 MAX_PROCS = 31  # rule masks are (1 << nr_procs) - 1 wide (GPUexplore.cu:980, 995)
 
@@ -143,8 +144,21 @@ def _field(words: Sequence[int], i: int, nbits: int) -> int:
     return (words[i // per] >> ((i % per) * nbits)) & ((1 << nbits) - 1)
 
 
-def encode(net: Network) -> List[int]:
-    """Encode a network as the integer lines of a gpf file."""
+def encode(net: Network, max_slots: Optional[int] = None, repeat_seed: Optional[int] = None) -> List[int]:
+    """Encode a network as the integer lines of a gpf file.
+
+    By default every transition entry is packed densely and every target is
+    written once, the form on which the reference's two successor kernels agree.
+    Two options write the other forms the format allows (same Network, same
+    successor sets under the intended semantics):
+
+    max_slots    at most this many targets per entry; the remaining slots stay 0,
+                 so one action's targets span more entries (max_buf_ints grows
+                 past 2) and an entry with empty slots is followed by another
+                 entry of the same action
+    repeat_seed  seeded: about a third of the target lists get one of their
+                 targets written a second time (the same successor twice)
+    """
     net.validate()
     n = net.nprocs
     bs = net.bits_state()
@@ -154,6 +168,13 @@ def encode(net: Network) -> List[int]:
     slots = [(31 - bits_act) // b for b in bs]
     if min(slots) < 1:
         raise ValueError("a process has too many local states for its transition entries")
+    per_entry = [min(k, max_slots) if max_slots else k for k in slots]
+    rng = random.Random(repeat_seed) if repeat_seed is not None else None
+
+    def with_repeats(targets: List[int]) -> List[int]:
+        if rng is None or rng.random() >= 1 / 3:
+            return targets
+        return targets + [rng.choice(targets)]
 
     trans: List[int] = []
     starts: List[List[int]] = []
@@ -165,18 +186,18 @@ def encode(net: Network) -> List[int]:
 
             def entries(sync_flag: int, act: int, targets: List[int]) -> int:
                 cnt = 0
-                for c in range(0, len(targets), slots[p]):
+                for c in range(0, len(targets), per_entry[p]):
                     e = sync_flag | (act << 1)
-                    for i, t in enumerate(targets[c:c + slots[p]]):
+                    for i, t in enumerate(targets[c:c + per_entry[p]]):
                         e |= (t + 1) << (1 + bits_act + i * bs[p])
                     trans.append(e)
                     cnt += 1
                 return cnt
 
             if net.local[p][s]:
-                entries(0, 0, list(net.local[p][s]))
+                entries(0, 0, with_repeats(list(net.local[p][s])))
             for a in sorted(net.sync[p][s]):
-                max_buf = max(max_buf, entries(1, a, list(net.sync[p][s][a])))
+                max_buf = max(max_buf, entries(1, a, with_repeats(list(net.sync[p][s][a]))))
         st.append(len(trans))
         starts.append(st)
 

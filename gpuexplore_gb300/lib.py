@@ -72,7 +72,7 @@ class Options(C.Structure):
         ("por", C.c_int32), ("cycle_proviso", C.c_int32), ("property", C.c_int32), ("device", C.c_int32),
         ("seed", C.c_uint64), ("max_states", C.c_uint64), ("store_states", C.c_uint64),
         ("collect_states", C.c_int32), ("bucket_bytes", C.c_int32),
-        ("launch_graph", C.c_int32), ("prune_commuting", C.c_int32),
+        ("launch_graph", C.c_int32), ("prune_commuting", C.c_int32), ("set_hash", C.c_int32),
     ]
 
 
@@ -88,7 +88,7 @@ class Result(C.Structure):
         ("inserts", C.c_uint64), ("evictions", C.c_uint64),
         ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("live_states", C.c_uint64), ("live_ms", C.c_double),
         ("live_rounds", C.c_uint64), ("table_generation", C.c_uint32), ("table_cleared", C.c_int32),
-        ("pruned", C.c_uint64),
+        ("pruned", C.c_uint64), ("overflowed", C.c_uint64), ("evict_ms", C.c_double),
     ]
 
 
@@ -103,7 +103,7 @@ class BatchItem(C.Structure):
     _fields_ = [
         ("status", C.c_int32), ("stopped", C.c_int32), ("verdict", C.c_int32), ("nlevels", C.c_uint32),
         ("states", C.c_uint64), ("set_hash", C.c_uint64), ("capacity", C.c_uint64),
-        ("completion_ms", C.c_double), ("admissions", C.c_uint32), ("reserved", C.c_uint32),
+        ("completion_ms", C.c_double), ("admissions", C.c_uint32), ("slot_bytes", C.c_uint32),
     ]
 
 
@@ -120,7 +120,8 @@ class BatchStats(C.Structure):
     _fields_ = [
         ("device_ms", C.c_double), ("states", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
         ("launches", C.c_uint32), ("claim", C.c_int32), ("threads", C.c_int32), ("blocks", C.c_int32),
-        ("load_factor", C.c_double), ("tune_ms", C.c_double),
+        ("load_factor", C.c_double), ("tune_ms", C.c_double), ("kernel_iters", C.c_int32),
+        ("instances_by_slot", C.c_uint32 * 3),
     ]
 
 
@@ -142,7 +143,7 @@ class DeviceInfo(C.Structure):
 
 
 _lib: Optional[C.CDLL] = None
-ABI_VERSION = 3
+ABI_VERSION = 4
 
 
 def load(path: str = LIB) -> C.CDLL:
@@ -209,12 +210,19 @@ class GpxError(RuntimeError):
         super().__init__(f"{what}: gpx status {status} ({name})")
 
 
+# Fields set on every options() call after gpx_options_init and before the
+# call's own keyword arguments (e.g. {"set_hash": 1} to get the visited-set
+# hash from every run of a process that compares runs).
+DEFAULT_OPTIONS: Dict[str, int] = {}
+
+
 def options(**kw) -> Options:
-    """Options with the library defaults, then the given fields (property may be a name)."""
+    """Options with the library defaults, then DEFAULT_OPTIONS, then the given
+    fields (property may be a name)."""
     lib = load()
     o = Options()
     lib.gpx_options_init(C.byref(o))
-    for k, v in kw.items():
+    for k, v in list(DEFAULT_OPTIONS.items()) + list(kw.items()):
         if k == "property" and isinstance(v, str):
             v = PROPERTIES[v]
         setattr(o, k, int(v))
@@ -275,7 +283,7 @@ def _result_dict(r: Result) -> Dict:
         "h2d_bytes": int(r.h2d_bytes), "d2h_bytes": int(r.d2h_bytes), "live_states": int(r.live_states),
         "live_ms": float(r.live_ms), "live_rounds": int(r.live_rounds),
         "table_generation": int(r.table_generation), "table_cleared": int(r.table_cleared),
-        "pruned": int(r.pruned),
+        "pruned": int(r.pruned), "overflowed": int(r.overflowed), "evict_ms": float(r.evict_ms),
         "expanded": int(r.expanded), "launches": int(r.launches), "explore_ms": float(r.explore_ms),
         "kernel_ms": float(r.kernel_ms), "setup_ms": float(r.setup_ms), "set_hash": f"{r.set_hash:016x}",
         "key_words": int(r.key_words), "table_count": int(r.table_count), "table_slots": int(r.table_slots),
@@ -385,14 +393,18 @@ def explore(path_or_model, check: bool = True, **kw) -> Dict:
 def explore_noalloc(model: Model, level_capacity: int = 1 << 16, check: bool = True, **kw) -> Dict:
     """gpx_explore_noalloc: the exploration with all device scratch in the library's
     static array (no allocation by the library).  The level counts land in a
-    caller-owned array; the result is not passed to gpx_result_free."""
+    caller-owned array; the result is not passed to gpx_result_free.  `levels`
+    holds the first min(nlevels, level_capacity) counts and `nlevels` the full
+    count the library reported, so a truncated list is visible."""
     lib = load()
     o = options(**kw)
     levels = (C.c_uint64 * max(1, level_capacity))()
     r = Result()
     rc = lib.gpx_explore_noalloc(model.handle, C.byref(o), levels, level_capacity, C.byref(r))
+    nlevels = int(r.nlevels)
     r.nlevels = min(r.nlevels, level_capacity)
     d = _result_dict(r) if rc == GPX_OK or r.level_counts else {"status": rc}
+    d["nlevels"] = nlevels
     if check and rc != GPX_OK:
         raise GpxError(rc, "exploring without allocation")
     d["rc"] = rc
@@ -463,8 +475,10 @@ def batch_explore(models: Sequence[Model], jobs: Sequence[Dict], level_capacity:
                     "verdict": VERDICTS.get(it.verdict, str(it.verdict)), "states": it.states,
                     "levels": [int(levels[k * level_capacity + l]) for l in range(nl)], "nlevels": it.nlevels,
                     "set_hash": f"{it.set_hash:016x}", "capacity": it.capacity,
-                    "completion_ms": it.completion_ms, "admissions": it.admissions})
+                    "completion_ms": it.completion_ms, "admissions": it.admissions,
+                    "slot_bytes": it.slot_bytes})
     stats = {f: getattr(st, f) for f, _ in BatchStats._fields_}
+    stats["instances_by_slot"] = list(st.instances_by_slot)
     stats["rc"] = rc
     del keep
     return out, stats

@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define GPX_ABI_VERSION 3
+#define GPX_ABI_VERSION 4
 
 /* Status codes.  They replace the reference's exit(1) paths. */
 typedef enum {
@@ -44,7 +44,9 @@ typedef enum {
     GPX_PROP_NONE = 0,
     GPX_PROP_DEADLOCK = 1, /* -d */
     GPX_PROP_SAFETY = 2,   /* -p: last process reaches local state 1 */
-    GPX_PROP_LIVENESS = 3  /* -p with gpf line 1 == 1; parsed, never checked (as in the reference) */
+    GPX_PROP_LIVENESS = 3  /* -p with gpf line 1 == 1: the reference parses it and checks nothing
+                              (GPUexplore.cu:1888-1898); here an accepting cycle through local state 1 of
+                              the last process is searched after a complete exploration without POR */
 } gpx_property;
 
 typedef enum {
@@ -81,6 +83,9 @@ typedef struct {
                                 inserted it and are led by a lower process -- a state of the same level
                                 generates each of them -- so fewer lookups reach the table; the visited
                                 set, level counts and verdicts are unchanged; 0: every successor */
+    int32_t set_hash;       /* 1: fill gpx_result.set_hash (one extra pass over the state store after the
+                               exploration, ~0.5 ms per 1.6e8 states: a check of the visited set against another
+                               explorer); 0 (gpx_options_init): skip the pass, set_hash = 0 */
 } gpx_options;
 
 /* Result of one exploration.  Arrays are owned by the library: gpx_result_free. */
@@ -97,7 +102,8 @@ typedef struct {
     uint64_t launches;       /* kernel launches of the exploration loop */
     double explore_ms;       /* device time of the exploration (CUDA events) */
     double setup_ms;         /* host time spent on table reset and model upload */
-    uint64_t set_hash;       /* order-independent hash of the visited set (sum of key hashes) */
+    uint64_t set_hash;       /* order-independent hash of the visited set (sum of key hashes); 0 unless
+                                gpx_options.set_hash */
     uint32_t key_words;      /* 32-bit words per state vector in `states_buf` */
     uint64_t table_count;    /* occupied hash-table slots, counted by a sweep like count_states
                                 (GPUexplore.cu:687-704); filled when collect_states or verbosity >= 2 */
@@ -123,6 +129,9 @@ typedef struct {
     uint64_t pruned;         /* successors not generated by commuting-move pruning (gpx_options.prune_commuting);
                                 with it, lookups/transitions/probes depend on which of a state's predecessors
                                 inserted it first and vary between runs */
+    uint64_t overflowed;     /* inserts that found all 32 probe buckets full; each was placed after its level's
+                                inserts, by all warps at once, with a chain of at most 4 displacements */
+    double evict_ms;         /* device time of those placement phases */
 } gpx_result;
 
 typedef struct gpx_model gpx_model;
@@ -227,12 +236,23 @@ int gpx_random_insert_probe(int device, uint64_t bytes, double *inserts_per_s);
  * min(nlevels, level_capacity) entries are written; result->nlevels is the full
  * count), states_buf stays NULL, no -v output is printed, and explore_ms /
  * kernel_ms are host wall-clock times.  Do not pass this result to
- * gpx_result_free.
+ * gpx_result_free.  No pinned host memory is used either: after each launch
+ * the control block (about 1 KB) is copied back into the call's own stack.
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call before
- * any stream capture.  Every call on a device shares the one array and leaves
- * its contents behind (each call clears what it needs cleared), so calls whose
- * GPU work overlaps -- from two host threads, or on two streams -- race. */
+ * any stream capture.  CUDA loads a library's kernels and reserves its static
+ * arrays lazily, on first use in a context (CUDA_MODULE_LOADING=LAZY, the
+ * default): if this call is the first use of libgpx on a device, the array is
+ * reserved inside it, so a caller under a memory cap makes one call (or any
+ * other libgpx call) on the device at set-up, while memory is still free.  The
+ * address is cached per device ordinal for the life of the process; after a
+ * cudaDeviceReset of that device it is stale and the library must not be used
+ * there again.  The work runs on the calling thread's per-thread default stream
+ * (cudaStreamPerThread: it does not wait for other blocking streams), and the
+ * call returns when it has finished.  Every call on a device shares the one
+ * array and leaves its contents behind (each call clears what it needs
+ * cleared), so calls whose GPU work overlaps -- from two host threads, or on two
+ * streams -- race. */
 #define GPX_NOALLOC_SCRATCH_BYTES (64u << 20)
 int gpx_explore_noalloc(const gpx_model *model, const gpx_options *opts, uint64_t *level_counts,
                         uint32_t level_capacity, gpx_result *result);
@@ -329,7 +349,7 @@ typedef struct {
     uint64_t capacity;      /* states admitted in the launch that finished it */
     double completion_ms;   /* device time from that launch's start to the instance's last level */
     uint32_t admissions;    /* launches the instance needed */
-    uint32_t reserved;
+    uint32_t slot_bytes;    /* its hash-slot width: 4, 8 or 16 bytes, the narrowest its state vector fits */
 } gpx_batch_item;
 
 typedef struct {
@@ -339,7 +359,8 @@ typedef struct {
     int32_t threads;        /* per block; 0 = 256 */
     int32_t claim;          /* states per work claim (the frontier tile); 0 = 64 */
     int32_t kernel_iters;   /* work claims per warp per launch (0 = until every instance is done) */
-    int32_t autotune;       /* choose claim, threads and load factor on a sample of the batch first */
+    int32_t autotune;       /* choose claim, threads, load factor, then kernel_iters on a sample of the batch
+                               first (the explicit values above are the starting point) */
     int32_t max_admissions; /* launches per instance before an overflow is final (0 = 3) */
     double load_factor;     /* table slots = admitted states / load_factor (0 = 0.5) */
     uint64_t seed;
@@ -358,6 +379,8 @@ typedef struct {
     int32_t claim, threads, blocks;
     double load_factor;
     double tune_ms;         /* host time spent autotuning */
+    int32_t kernel_iters;   /* claims per warp per launch that ran (tuned with autotune) */
+    uint32_t instances_by_slot[3]; /* instances with 32-, 64- and 128-bit slots */
 } gpx_batch_stats;
 
 void gpx_batch_options_init(gpx_batch_options *opts);

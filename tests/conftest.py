@@ -22,9 +22,12 @@ def built():
 
 @pytest.fixture(scope="session")
 def gpu(built):
-    """The library on a GPU; the CUDA path must load and find a device."""
+    """The library on a GPU; the CUDA path must load and find a device.  Every
+    run of the GPU tests computes the visited-set hash (off by default in the
+    library), which the tests compare with the oracle's."""
     from gpuexplore_gb300 import lib
     lib.load()
+    lib.DEFAULT_OPTIONS["set_hash"] = 1
     if lib.device_info(0) is None:
         pytest.fail("no CUDA device visible to libgpx")
     return lib

@@ -44,6 +44,8 @@ def _check(lib, tmp_path, cases, **opts):
     items, stats = lib.batch_explore(models, jobs, level_capacity=4096, **opts)
     for k, (it, w) in enumerate(zip(items, want)):
         assert it["status"] == 0, (k, it)
+        bits = cases[k][0].firstbit()[-1]  # each instance gets the narrowest slot its vector fits
+        assert it["slot_bytes"] == (4 if bits <= 31 else (8 if bits <= 63 else 16)), (k, bits)
         assert it["nlevels"] == len(w["levels"]), k
         for key in ("states", "levels", "verdict", "stopped", "set_hash"):
             assert it[key] == w[key], (k, cases[k][1], key, it[key], w[key])
@@ -89,3 +91,28 @@ def test_batch_pruning_on_and_off(gpu, tmp_path):
     assert len(cases) >= 6
     _check(gpu, tmp_path, cases)
     _check(gpu, tmp_path, cases, prune_commuting=0)
+
+
+def test_batch_eviction_instead_of_readmission(gpu, tmp_path):
+    """Partitions at a 0.95 load factor: inserts whose probe sequence is full are
+    placed with eviction by the warp that closes the level, so the instances
+    finish in their first admission with results equal to the oracle's."""
+    cases = []
+    for k in range(6):
+        net = gen.random_network(300 + k, nprocs=20, states=(3, 5), outdeg=(1, 2), safety=False)
+        cases.append((net, ["plain", "deadlock", "por_proviso"][k % 3], 0))
+    models, jobs, want = [], [], []
+    for k, (net, fs, _) in enumerate(cases):
+        path = write_net(net, tmp_path, f"e{k}")
+        cli, kw = FLAGS[fs]
+        w = oracle(path, cli, max_states=60_000)
+        want.append(w)
+        jobs.append({"property": kw.get("property", "none"), "por": kw.get("por", 0),
+                     "cycle_proviso": kw.get("cycle_proviso", 0), "max_states": 60_000,
+                     "capacity": w["states"] + 16})
+        models.append(gpu.Model.from_file(path))
+    items, stats = gpu.batch_explore(models, jobs, level_capacity=4096, load_factor=0.95)
+    for k, (it, w) in enumerate(zip(items, want)):
+        assert it["status"] == 0 and it["admissions"] == 1, (k, it)
+        for key in ("states", "levels", "verdict", "stopped", "set_hash"):
+            assert it[key] == w[key], (k, key)

@@ -62,7 +62,7 @@ def test_status_strings(built):
     from gpuexplore_gb300 import lib
     L = lib.load()
     assert L.gpx_status_string(4) == b"problem with hash table"
-    assert L.gpx_abi_version() == 3
+    assert L.gpx_abi_version() == lib.ABI_VERSION == 4
 
 
 def test_no_gpu_is_a_status(built, tmp_path):
@@ -99,17 +99,28 @@ def test_option_validation_before_device(built, tmp_path):
     from gpuexplore_gb300 import lib
     p = tmp_path / "m.gpf"
     gpf.write(gen.ring(1), str(p))
-    for bad in (dict(por=5), dict(por=-1), dict(bucket_bytes=64)):
+    bads = (dict(por=5), dict(por=-1), dict(bucket_bytes=64), dict(property=7), dict(threads=48),
+            dict(threads=512), dict(q_words=1 << 62), dict(store_states=1 << 62))
+    for bad in bads:
         r = lib.explore(str(p), check=False, **bad)
         assert r["rc"] == 6, bad  # GPX_ERR_INVALID
+    # the allocation-free entry point refuses the same options the same way
+    m = lib.Model.from_file(str(p))
+    try:
+        for bad in bads:
+            r = lib.explore_noalloc(m, check=False, **bad)
+            assert r["rc"] == 6, bad
+    finally:
+        m.close()
 
 
 def test_option_defaults(built):
     from gpuexplore_gb300 import lib
-    o = lib.options()
-    assert o.launch_graph == 1 and o.por == 0 and o.kernel_iters == 0 and o.bucket_bytes == 0
-    assert o.prune_commuting == 1
     L = lib.load()
+    o = lib.Options()
+    L.gpx_options_init(lib.C.byref(o))
+    assert o.launch_graph == 1 and o.por == 0 and o.kernel_iters == 0 and o.bucket_bytes == 0
+    assert o.prune_commuting == 1 and o.set_hash == 0 and o.struct_size == lib.C.sizeof(lib.Options)
     b = lib.BatchOptions()
     L.gpx_batch_options_init(lib.C.byref(b))
     assert b.latency_sms == -1 and b.struct_size == lib.C.sizeof(lib.BatchOptions)
