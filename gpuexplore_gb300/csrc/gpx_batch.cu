@@ -91,6 +91,13 @@ static __device__ __forceinline__ unsigned long long vload64(const unsigned long
     return *(volatile const unsigned long long *)p;
 }
 
+// Acquire load of a ticket: the level it names is read after it.
+static __device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
 static __device__ BLevel read_level(const BInst *I, unsigned int e) {
     const volatile BLevel *L = &I->lvl[e & 1];
     BLevel r;
@@ -228,73 +235,94 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(BParams BP) {
         if (vload(&BP.g->done_count) >= BP.count || vload(&BP.g->error)) break;
         if (BP.max_claims && claims >= BP.max_claims) break;
         bool worked = false;
-        for (uint32_t k = 0; k < (express ? 2 * BP.count : BP.count) && !worked; k++) {
-            // a reserved SM's warp scans twice: critical phases only, then any phase
-            const bool any = k >= BP.count;
-            uint32_t i = next + (any ? k - BP.count : k);
-            if (i >= BP.count) i -= BP.count;
-            BInst *I = &BP.inst[i];
-            if (vload(&I->ctrl.done)) continue;
-            unsigned long long t = vload64(&I->ticket);
-            unsigned int e = (unsigned int)(t >> 40);
-            __threadfence();
-            BLevel L = read_level(I, e);
-            unsigned long long n = L.hi - L.lo;
-            if ((t & kCurMask) >= n) continue;
-            if (BP.latency_sms) {
-                const bool critical = n <= kCriticalStates && e >= kCriticalEpochs;
-                if (express ? (!critical && !any) : critical) continue;
-            }
-            // level-sized claims (at least the tuned size) keep few-state levels on many warps
-            unsigned long long claim = n / ((unsigned long long)BP.total_warps * 4ull);
-            claim = claim < BP.claim ? BP.claim : (claim > 4096 ? 4096 : claim);
-            unsigned long long old = 0;
-            if (lane == 0) old = atomicAdd(&I->ticket, claim);
-            old = __shfl_sync(kFull, old, 0);
-            unsigned int e2 = (unsigned int)(old >> 40);
-            unsigned long long cur = old & kCurMask;
-            if (e2 != e) {
-                __threadfence();
-                L = read_level(I, e2);
-                n = L.hi - L.lo;
-            }
-            if (cur >= n) continue;
-            unsigned long long cnt = (n - cur) < claim ? (n - cur) : claim;
-            bool decide = L.phase == PH_DECIDE;
-            if (I->kind == 0)
-                run_claim<K32>(BP, I, raw, L.lo, cur, cnt, claim, decide);
-            else if (I->kind == 1)
-                run_claim<K64>(BP, I, raw, L.lo, cur, cnt, claim, decide);
-            else
-                run_claim<K128>(BP, I, raw, L.lo, cur, cnt, claim, decide);
-            __threadfence();
-            unsigned long long d = 0;
-            if (lane == 0) d = atomicAdd(&I->completed[e2 & 1], cnt) + cnt;
-            if (__shfl_sync(kFull, d, 0) == n) {
-                // every chunk of the epoch is done: the instance is quiescent.  Keys
-                // whose probe sequence was full are placed with eviction first.
-                __threadfence();
-                Ctrl *c = &I->ctrl;
-                const unsigned long long over = vload(&c->overflow_count);
-                if (over) {
-                    if (over <= I->overflow_cap && !vload(&c->error)) {
-                        if (I->kind == 0)
-                            place_instance<K32>(BP, I, over, lane);
-                        else if (I->kind == 1)
-                            place_instance<K64>(BP, I, over, lane);
-                        else
-                            place_instance<K128>(BP, I, over, lane);
-                    } else if (lane == 0)
-                        set_error(c, GPX_ERR_TABLE_FULL); // re-admitted with a larger partition
-                    if (lane == 0) c->overflow_count = 0;
-                    __threadfence();
+        // The lanes scan 32 instances at a time for a claimable phase (a reserved
+        // SM's warp scans the virtual range twice: critical phases only, then any),
+        // then the warp tries the candidates in scan order.  A serial scan with a
+        // fence per instance took a millisecond over 512 instances.
+        const uint32_t span = express ? 2 * BP.count : BP.count;
+        for (uint32_t k0 = 0; k0 < span && !worked; k0 += 32) {
+            const uint32_t k = k0 + lane;
+            uint32_t i = 0;
+            bool cand = false;
+            if (k < span) {
+                const bool any = k >= BP.count;
+                i = next + (any ? k - BP.count : k);
+                if (i >= BP.count) i -= BP.count;
+                const BInst *Ic = &BP.inst[i];
+                if (!vload(&Ic->ctrl.done)) {
+                    const unsigned long long t = ld_acquire64(&Ic->ticket);
+                    const unsigned int e = (unsigned int)(t >> 40);
+                    const BLevel Lc = read_level(Ic, e);
+                    const unsigned long long n = Lc.hi - Lc.lo;
+                    cand = (t & kCurMask) < n;
+                    if (cand && BP.latency_sms) {
+                        const bool critical = n <= kCriticalStates && e >= kCriticalEpochs;
+                        if (express ? (!critical && !any) : critical) cand = false;
+                    }
                 }
-                if (lane == 0) close_instance(BP, I, e2);
             }
-            __syncwarp();
-            worked = true;
-            next = i;
-            claims++;
+            uint32_t m = __ballot_sync(kFull, cand);
+            while (m && !worked) {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                const uint32_t ci = __shfl_sync(kFull, i, src); // this candidate (i stays per lane)
+                BInst *I = &BP.inst[ci];
+                unsigned long long t = ld_acquire64(&I->ticket);
+                unsigned int e = (unsigned int)(t >> 40);
+                BLevel L = read_level(I, e);
+                unsigned long long n = L.hi - L.lo;
+                if ((t & kCurMask) >= n) continue;
+                // level-sized claims (at least the tuned size) keep few-state levels on many warps
+                unsigned long long claim = n / ((unsigned long long)BP.total_warps * 4ull);
+                claim = claim < BP.claim ? BP.claim : (claim > 4096 ? 4096 : claim);
+                unsigned long long old = 0;
+                if (lane == 0) old = atomicAdd(&I->ticket, claim);
+                old = __shfl_sync(kFull, old, 0);
+                unsigned int e2 = (unsigned int)(old >> 40);
+                unsigned long long cur = old & kCurMask;
+                if (e2 != e) {
+                    __threadfence();
+                    L = read_level(I, e2);
+                    n = L.hi - L.lo;
+                }
+                if (cur >= n) continue;
+                unsigned long long cnt = (n - cur) < claim ? (n - cur) : claim;
+                bool decide = L.phase == PH_DECIDE;
+                if (I->kind == 0)
+                    run_claim<K32>(BP, I, raw, L.lo, cur, cnt, claim, decide);
+                else if (I->kind == 1)
+                    run_claim<K64>(BP, I, raw, L.lo, cur, cnt, claim, decide);
+                else
+                    run_claim<K128>(BP, I, raw, L.lo, cur, cnt, claim, decide);
+                __threadfence();
+                unsigned long long d = 0;
+                if (lane == 0) d = atomicAdd(&I->completed[e2 & 1], cnt) + cnt;
+                if (__shfl_sync(kFull, d, 0) == n) {
+                    // every chunk of the epoch is done: the instance is quiescent.  Keys
+                    // whose probe sequence was full are placed with eviction first.
+                    __threadfence();
+                    Ctrl *c = &I->ctrl;
+                    const unsigned long long over = vload(&c->overflow_count);
+                    if (over) {
+                        if (over <= I->overflow_cap && !vload(&c->error)) {
+                            if (I->kind == 0)
+                                place_instance<K32>(BP, I, over, lane);
+                            else if (I->kind == 1)
+                                place_instance<K64>(BP, I, over, lane);
+                            else
+                                place_instance<K128>(BP, I, over, lane);
+                        } else if (lane == 0)
+                            set_error(c, GPX_ERR_TABLE_FULL); // re-admitted with a larger partition
+                        if (lane == 0) c->overflow_count = 0;
+                        __threadfence();
+                    }
+                    if (lane == 0) close_instance(BP, I, e2);
+                }
+                __syncwarp();
+                worked = true;
+                next = ci;
+                claims++;
+            }
         }
         if (worked) {
             idle_since = 0;
@@ -396,6 +424,7 @@ namespace {
 struct BatchConfig {
     int blocks, threads, claim, kernel_iters, latency_sms;
     bool prune_commuting;
+    bool narrow_slots; // each instance in the narrowest slot its vector fits (else 128-bit slots for all)
     double load_factor;
 };
 
@@ -410,17 +439,23 @@ struct Outcome {
 constexpr unsigned long long kInstOverflow = 1024; // overflowed keys an instance can place per level
 constexpr uint32_t kSlotBytes[3] = {4, 8, 16};
 
-// Slot width of an instance: the narrowest that holds its state vector and the
-// occupancy bit of each 32/64-bit half (as in a single-network table).
-uint32_t slot_kind(const gpx_model *m) {
+// Slot width of an instance: with narrow slots the narrowest that holds its
+// state vector and the occupancy bit of each 32/64-bit half (as in a
+// single-network table), else 128 bits.  Narrow slots hold two to four times
+// the states per byte; 128-bit slots (two per bucket) measured faster on the
+// config-5 batch (432 vs 470 ms, p50 15 vs 27 ms): a small instance's 8-slot
+// buckets put more concurrent inserts on each sector.
+uint32_t slot_kind(const gpx_model *m, bool narrow) {
     const uint32_t bits = m->dec.state_bits;
+    if (!narrow) return 2u;
     return bits <= 31 ? 0u : (bits <= 63 ? 1u : 2u);
 }
 
 // Device bytes per admitted state: table slots at the load factor, the store
 // slot and the per-state cluster / label word.
-double bytes_per_state(const gpx_model *m, double load_factor) {
-    const double sb = kSlotBytes[slot_kind(m)];
+double bytes_per_state(const gpx_model *m, const BatchConfig &cfg) {
+    const double load_factor = cfg.load_factor;
+    const double sb = kSlotBytes[slot_kind(m, cfg.narrow_slots)];
     return sb / load_factor + sb + 4.0;
 }
 
@@ -516,7 +551,7 @@ int run_launch(int device, const cudaDeviceProp &prop, const BatchConfig &cfg, u
     size_t over_bytes = 0;
     for (uint32_t k = 0; k < count; k++) {
         const gpx_model *m = models[idx[k]];
-        const uint32_t kind = slot_kind(m), sb = kSlotBytes[kind], per_bucket = 32 / sb;
+        const uint32_t kind = slot_kind(m, cfg.narrow_slots), sb = kSlotBytes[kind], per_bucket = 32 / sb;
         uint64_t slots = (uint64_t)((double)cap[k] / cfg.load_factor) + 4;
         uint64_t nb = (slots + per_bucket - 1) / per_bucket;
         nb = (nb + 1) & ~1ull; // even: buckets are probed in pairs
@@ -721,7 +756,8 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
     BatchConfig cfg;
     cfg.blocks = opts->blocks;
     cfg.threads = opts->threads > 0 ? opts->threads : 256;
-    cfg.claim = opts->claim > 0 ? opts->claim : 64;
+    cfg.claim = opts->claim > 0 ? opts->claim : 8;
+    cfg.narrow_slots = opts->narrow_slots != 0;
     cfg.kernel_iters = opts->kernel_iters;
     cfg.load_factor = opts->load_factor > 0 ? opts->load_factor : 0.5;
     // automatic: about a tenth of the SMs (16 of 152 measured best on config 5, with 8
@@ -758,7 +794,7 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return GPX_ERR_CUDA;
         double want = 0;
-        for (uint32_t i : todo) want += (double)cap[i] * bytes_per_state(models[i], cfg.load_factor);
+        for (uint32_t i : todo) want += (double)cap[i] * bytes_per_state(models[i], cfg);
         const double room = 0.7 * (double)free_b;
         if (want > room)
             for (uint32_t i : todo) cap[i] = std::max<uint64_t>(1024, (uint64_t)((double)cap[i] * room / want));
@@ -818,6 +854,19 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
                 bestc = c;
             }
         }
+        {   // then the slot policy: narrow slots save memory, 128-bit slots are often faster
+            BatchConfig c = bestc;
+            c.narrow_slots = !bestc.narrow_slots;
+            std::vector<Outcome> o;
+            float ms = 0;
+            uint32_t l = 0;
+            if (run_launch(opts->device, prop, c, opts->seed, models, jobs, sample, scap, d_por, &o, &ms, &l) ==
+                    GPX_OK &&
+                ms < best) {
+                best = ms;
+                bestc = c;
+            }
+        }
         cfg = bestc;
         st.tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
@@ -830,7 +879,7 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
             size_t free_b = 0, total_b = 0;
             cudaMemGetInfo(&free_b, &total_b);
             double want = 0;
-            for (uint32_t i : todo) want += (double)cap[i] * bytes_per_state(models[i], cfg.load_factor);
+            for (uint32_t i : todo) want += (double)cap[i] * bytes_per_state(models[i], cfg);
             const double room = 0.7 * (double)free_b;
             double scale = want > room ? room / want : 1.0;
             for (uint32_t i : todo) c2.push_back(std::max<uint64_t>(1024, (uint64_t)((double)cap[i] * scale)));
@@ -854,7 +903,7 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
             it.set_hash = o.set_hash;
             it.capacity = o.capacity;
             it.completion_ms = o.completion_ms;
-            it.slot_bytes = kSlotBytes[slot_kind(models[i])];
+            it.slot_bytes = kSlotBytes[slot_kind(models[i], cfg.narrow_slots)];
             if (adm == 1 && o.status == GPX_OK) completion.push_back(o.completion_ms);
             if (level_counts && level_capacity)
                 for (uint32_t l = 0; l < std::min<uint32_t>(level_capacity, (uint32_t)o.levels.size()); l++)
@@ -878,6 +927,7 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
     st.blocks = cfg.blocks;
     st.load_factor = cfg.load_factor;
     st.kernel_iters = cfg.kernel_iters;
+    st.narrow_slots = cfg.narrow_slots ? 1 : 0;
     for (uint32_t i = 0; i < count; i++)
         if (items[i].slot_bytes) st.instances_by_slot[items[i].slot_bytes == 4 ? 0 : (items[i].slot_bytes == 8 ? 1 : 2)]++;
     if (stats) *stats = st;

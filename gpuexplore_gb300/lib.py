@@ -112,7 +112,7 @@ class BatchOptions(C.Structure):
         ("struct_size", C.c_uint32), ("device", C.c_int32), ("blocks", C.c_int32), ("threads", C.c_int32),
         ("claim", C.c_int32), ("kernel_iters", C.c_int32), ("autotune", C.c_int32), ("max_admissions", C.c_int32),
         ("load_factor", C.c_double), ("seed", C.c_uint64), ("por_model", C.c_void_p),
-        ("latency_sms", C.c_int32), ("prune_commuting", C.c_int32),
+        ("latency_sms", C.c_int32), ("prune_commuting", C.c_int32), ("narrow_slots", C.c_int32),
     ]
 
 
@@ -121,7 +121,7 @@ class BatchStats(C.Structure):
         ("device_ms", C.c_double), ("states", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
         ("launches", C.c_uint32), ("claim", C.c_int32), ("threads", C.c_int32), ("blocks", C.c_int32),
         ("load_factor", C.c_double), ("tune_ms", C.c_double), ("kernel_iters", C.c_int32),
-        ("instances_by_slot", C.c_uint32 * 3),
+        ("instances_by_slot", C.c_uint32 * 3), ("narrow_slots", C.c_int32),
     ]
 
 

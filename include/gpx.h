@@ -357,10 +357,11 @@ typedef struct {
     int32_t device;
     int32_t blocks;         /* 0: every SM at full occupancy */
     int32_t threads;        /* per block; 0 = 256 */
-    int32_t claim;          /* states per work claim (the frontier tile); 0 = 64 */
+    int32_t claim;          /* states per work claim (the frontier tile) at least; 0 = 8 (claims grow with
+                               a level: a quarter of a fair share per warp, up to 4096) */
     int32_t kernel_iters;   /* work claims per warp per launch (0 = until every instance is done) */
-    int32_t autotune;       /* choose claim, threads, load factor, then kernel_iters on a sample of the batch
-                               first (the explicit values above are the starting point) */
+    int32_t autotune;       /* choose claim, threads, load factor, then kernel_iters, then the slot policy on a
+                               sample of the batch first (the explicit values above are the starting point) */
     int32_t max_admissions; /* launches per instance before an overflow is final (0 = 3) */
     double load_factor;     /* table slots = admitted states / load_factor (0 = 0.5) */
     uint64_t seed;
@@ -369,6 +370,10 @@ typedef struct {
                                -1 (gpx_batch_options_init) = a tenth of the SMs, 0 = none */
     int32_t prune_commuting; /* 1 (gpx_batch_options_init): plain instances prune commuting moves
                                 (gpx_options.prune_commuting); 0: every successor */
+    int32_t narrow_slots;   /* 1: each instance gets the narrowest hash slot its state vector fits (32, 64 or
+                               128 bits: two to four times the states per byte for small networks); 0
+                               (gpx_batch_options_init): 128-bit slots for every instance (two per bucket, fewer
+                               concurrent inserts per sector: faster on many small instances) */
 } gpx_batch_options;
 
 typedef struct {
@@ -381,6 +386,7 @@ typedef struct {
     double tune_ms;         /* host time spent autotuning */
     int32_t kernel_iters;   /* claims per warp per launch that ran (tuned with autotune) */
     uint32_t instances_by_slot[3]; /* instances with 32-, 64- and 128-bit slots */
+    int32_t narrow_slots;   /* the slot policy that ran (tuned with autotune) */
 } gpx_batch_stats;
 
 void gpx_batch_options_init(gpx_batch_options *opts);
