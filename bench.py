@@ -50,7 +50,7 @@ BUDGET = W.CONFIG2_BUDGET
 Q_WORDS = W.CONFIG2_Q_WORDS
 CPU_SAMPLE_BUDGET = W.CONFIG2_SAMPLE_BUDGET  # the first 9 BFS levels (38.8M states)
 WORKLOAD = "config-2 random gpf network (16 procs + monitor, seed 2024), -d, BFS to 1e8-state budget"
-KERNEL_BUILD = "guided-claims-v8-prune-v4u64"  # names the kernel version a committed traffic capture belongs to
+KERNEL_BUILD = "place-kernel-v1"  # names the kernel version a committed traffic capture belongs to
 
 
 def measured_peaks():
@@ -301,10 +301,11 @@ def run_other_workload(args, local):
             desc = "config-1 rings of 8 processes x 5 states, seeds 1-10, -d, 2^22-word table"
         else:
             nets = W.config3_networks()
-            kw = dict(W.PROPERTY_FLAGS["por_proviso"][1], q_words=W.CONFIG3_Q_WORDS,
-                      max_states=min(args.budget, W.CONFIG3_BUDGET))
+            kw = dict(W.PROPERTY_FLAGS["por_proviso"][1], q_words=args.q_words or W.CONFIG3_Q_WORDS,
+                      max_states=args.budget or W.CONFIG3_BUDGET)
             desc = "config-3 clustered networks (24 processes, 4-6 clusters), seeds 1-3, --por --cycle-proviso"
         models = [lib.Model.from_words(gpf.encode(n)) for n in nets]
+        kw["launch_graph"] = 0 if args.no_graph else 1
         ex = lib.Explorer(models[0], lib.options(device=local, **kw))
         for _ in range(args.warmup):
             for m in models:
@@ -404,9 +405,10 @@ def main():
     ap.add_argument("--no-graph", action="store_true",
                     help="launch the exploration kernels from the host loop instead of one CUDA graph per run "
                          "(same kernels; used for the ncu captures)")
-    ap.add_argument("--budget", type=int, default=BUDGET,
+    ap.add_argument("--budget", type=int, default=None,
                     help="state budget (smaller values give the profiling cases of the same network)")
-    ap.add_argument("--q-words", type=int, default=Q_WORDS, help="hash table size in 32-bit words")
+    ap.add_argument("--q-words", type=int, default=None,
+                    help="hash table size in 32-bit words (default: the workload's own)")
     ap.add_argument("--store-states", type=int, default=0, help="state store capacity (0: table slots)")
     ap.add_argument("--workload", default="config2",
                     choices=["config1", "config2", "config3", "config4", "config5", "liveness"],
@@ -417,6 +419,9 @@ def main():
     ap.add_argument("--val-seeds", type=int, default=60)
     ap.add_argument("--eval-budget", type=int, default=2_000_000)
     args = ap.parse_args()
+    if args.workload == "config2":
+        args.budget = args.budget or BUDGET
+        args.q_words = args.q_words or Q_WORDS
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
