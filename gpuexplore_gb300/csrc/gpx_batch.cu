@@ -231,6 +231,7 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(BParams BP) {
     uint32_t next = gwarp % BP.count;
     uint32_t claims = 0;
     uint64_t idle_since = 0;
+    unsigned int idle_ns = 256;
     for (;;) {
         if (vload(&BP.g->done_count) >= BP.count || vload(&BP.g->error)) break;
         if (BP.max_claims && claims >= BP.max_claims) break;
@@ -326,9 +327,14 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(BParams BP) {
         }
         if (worked) {
             idle_since = 0;
+            idle_ns = 256;
         } else {
-            // nothing claimable right now: other warps are finishing levels
-            __nanosleep(512);
+            // nothing claimable right now: other warps are finishing levels.  The
+            // sleep doubles up to 8 us, so that thousands of idle warps do not
+            // keep polling the few tickets the busy ones claim from (ten rings
+            // in one batch: 1.51 -> 1.18 ms)
+            __nanosleep(idle_ns);
+            if (idle_ns < 8192) idle_ns <<= 1;
             uint64_t now = globaltimer();
             if (!idle_since)
                 idle_since = now;

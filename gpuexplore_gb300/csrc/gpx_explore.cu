@@ -85,22 +85,29 @@ template <class K, int MODE> __device__ void close_phase(const Params &P) {
         set_error(c, GPX_ERR_TABLE_FULL); // more keys than the overflow list holds
         c->overflow_count = 0;
     }
-    unsigned long long hi = c->hi;
-    unsigned long long newhi = c->store_count;
+    // the fields the decision reads, loaded together before any store
+    const unsigned long long hi = c->hi, sc = c->store_count;
+    const unsigned int nlev = c->nlevels, lvl = c->level, ll = c->launch_levels, err0 = c->error,
+                       viol = c->violation;
+    unsigned long long newhi = sc;
     if (newhi > P.store_cap) newhi = P.store_cap;
     unsigned long long cnt = newhi - hi;
+    unsigned int err = err0;
     if (cnt) {
-        if (c->nlevels < kMaxLevels)
-            P.levels[c->nlevels++] = cnt;
-        else
+        if (nlev < kMaxLevels) {
+            P.levels[nlev] = cnt;
+            c->nlevels = nlev + 1;
+        } else {
             set_error(c, GPX_ERR_UNSUPPORTED);
+            err = GPX_ERR_UNSUPPORTED;
+        }
     }
-    c->level++;
-    c->launch_levels++;
-    if (c->error) {
+    c->level = lvl + 1;
+    c->launch_levels = ll + 1;
+    if (err) {
         c->done = 1;
         c->stop = GPX_STOP_ERROR;
-    } else if (c->violation) {
+    } else if (viol) {
         c->done = 1;
         c->stop = GPX_STOP_VIOLATION;
     } else if (cnt == 0) {
@@ -118,7 +125,7 @@ template <class K, int MODE> __device__ void close_phase(const Params &P) {
     // spread over every warp instead of queueing behind a few long batches
     unsigned long long per = cnt / ((unsigned long long)P.total_warps * 4ull);
     c->claim = (unsigned int)(per < 1 ? 1 : (per > 4096 ? 4096 : per));
-    if (P.levels_per_launch && c->launch_levels >= P.levels_per_launch && !c->done) c->pause = 1;
+    if (P.levels_per_launch && ll + 1 >= P.levels_per_launch && !c->done) c->pause = 1;
 }
 
 // What a block needs of the current phase, read from the control block once
@@ -144,19 +151,32 @@ template <class K, int MODE> __device__ void grid_barrier(const Params &P, Level
     if (threadIdx.x == 0) {
         Ctrl *c = P.ctrl;
         unsigned int gen = vload(&c->bar_gen);
-        __threadfence();
-        unsigned int arrived = atomicAdd(&c->bar_count, 1u);
+        // The arrival releases this block's writes of the phase (its warps'
+        // writes are ordered before it by the block barrier) and acquires the
+        // earlier arrivals'; the closer's release of bar_gen publishes the
+        // close to the waiters' acquire loads.  (Full fences around plain
+        // atomics did the same, 2.5% slower per level on config 1.)
+        unsigned int arrived;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(arrived) : "l"(&c->bar_count) : "memory");
         if (arrived == gridDim.x - 1) {
-            __threadfence();
             close_phase<K, MODE>(P);
             c->bar_count = 0;
-            __threadfence();
-            atomicAdd(&c->bar_gen, 1u);
-        } else if (!wait_change(&c->bar_gen, gen, P.timeout_ns, 512)) {
-            set_error(c, GPX_ERR_TIMEOUT);
-            atomicMax(&c->timeout_at, 1u);
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" :: "l"(&c->bar_gen) : "memory");
+        } else { // bounded wait for the close
+            uint64_t t0 = globaltimer();
+            unsigned int ns = 32, g;
+            for (;;) {
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(&c->bar_gen) : "memory");
+                if (g != gen) break;
+                __nanosleep(ns);
+                if (ns < 512) ns <<= 1;
+                if (globaltimer() - t0 > P.timeout_ns) {
+                    set_error(c, GPX_ERR_TIMEOUT);
+                    atomicMax(&c->timeout_at, 1u);
+                    break;
+                }
+            }
         }
-        __threadfence();
         read_view(c, view);
     }
     __syncthreads();
