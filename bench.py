@@ -312,6 +312,7 @@ def run_other_workload(args, local):
                 ex.set_model(m)
                 ex.run()
         ms, states, kms = 0.0, 0, 0.0
+        probes = inserts = lookups = 0
         for _ in range(args.steps):
             for m in models:
                 ex.set_model(m)
@@ -319,7 +320,20 @@ def run_other_workload(args, local):
                 ms += r["setup_ms"] + r["kernel_ms"]
                 kms += r["kernel_ms"]
                 states += r["states"]
-        extra = {}
+                probes += r["probes"]
+                inserts += r["inserts"]
+                lookups += r["lookups"]
+        extra = {"lookups_per_step": lookups // args.steps, "probes_per_step": probes // args.steps,
+                 "inserts_per_step": inserts // args.steps}
+        if args.workload == "config3":
+            # the table's random-access floor, as for the headline: every insert is a
+            # read + CAS of a random bucket, every other probe (the decide pass's
+            # lookups, mostly) a random 32-byte gather; the table is 10 GB
+            gathers = lib.random_gather_rate(local, 20 << 30)
+            rmw = lib.random_insert_rate(local, 20 << 30)
+            floor = (inserts / rmw + max(0, probes - inserts) / gathers) * 1000.0 / args.steps
+            extra["random_access"] = {"floor_ms": floor, "frac": floor / (kms / args.steps),
+                                      "peak_gathers_per_s": gathers, "peak_inserts_per_s": rmw}
         if args.workload == "config1":
             # the same ten rings in one batched launch (gpx_batch_explore); the first
             # warm-up call autotunes, the timed calls reuse what it chose
@@ -333,8 +347,8 @@ def run_other_workload(args, local):
                 items, st = lib.batch_explore(models, jobs, **tuned)
                 bms += st["device_ms"]
                 bst += st["states"]
-            extra = {"batched_states_per_s": bst / (bms / 1000.0), "batched_ms_per_step": bms / args.steps,
-                     "batched_tuned": tuned}
+            extra.update({"batched_states_per_s": bst / (bms / 1000.0), "batched_ms_per_step": bms / args.steps,
+                          "batched_tuned": tuned})
         else:
             # the other reductions on the same networks: states kept and device time
             ex.close()
