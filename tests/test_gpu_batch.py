@@ -119,3 +119,26 @@ def test_batch_eviction_instead_of_readmission(gpu, tmp_path):
         assert it["status"] == 0 and it["admissions"] == 1, (k, it)
         for key in ("states", "levels", "verdict", "stopped", "set_hash"):
             assert it[key] == w[key], (k, key)
+
+
+def test_batch_eviction_narrow_slots(gpu, tmp_path):
+    """The closing warp's placement on 32- and 64-bit slots (narrow_slots) at a
+    0.95 load factor: first admission, oracle results."""
+    cases = []
+    for k, (seed, n) in enumerate(((50, 10), (53, 10), (45, 11), (43, 14))):  # 21K-78K states each
+        net = gen.random_network(seed, nprocs=n, states=(3, 6), outdeg=(1, 2), safety=False)
+        cases.append((net, ["plain", "deadlock"][k % 2], 0))
+    models, jobs, want = [], [], []
+    for k, (net, fs, _) in enumerate(cases):
+        path = write_net(net, tmp_path, f"n{k}")
+        cli, kw = FLAGS[fs]
+        w = oracle(path, cli, max_states=100_000)
+        want.append(w)
+        jobs.append({"property": kw.get("property", "none"), "max_states": 100_000, "capacity": w["states"] + 16})
+        models.append(gpu.Model.from_file(path))
+    items, stats = gpu.batch_explore(models, jobs, level_capacity=4096, load_factor=0.95, narrow_slots=1)
+    assert stats["narrow_slots"] == 1 and set(it["slot_bytes"] for it in items) <= {4, 8}
+    for k, (it, w) in enumerate(zip(items, want)):
+        assert it["status"] == 0 and it["admissions"] == 1, (k, it)
+        for key in ("states", "levels", "verdict", "stopped", "set_hash"):
+            assert it[key] == w[key], (k, key)

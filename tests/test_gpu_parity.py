@@ -144,3 +144,21 @@ def test_width_boundaries(gpu, tmp_path, bits, flags):
     _same(o, g)
     assert g["slot_bytes"] == (4 if bits <= 31 else (8 if bits <= 63 else 16))
     assert g["table_generation"] == (1 if 64 <= bits <= 112 else 0)
+
+
+@pytest.mark.parametrize("seed,nprocs,width,slots_per_state", [(45, 11, 4, 1.01), (43, 14, 8, 1.02)])
+def test_high_load_eviction_narrow_slots(gpu, tmp_path, seed, nprocs, width, slots_per_state):
+    """Placement with eviction on 32- and 64-bit slots (8 and 4 per bucket, so
+    longer probe sequences: 98-99% load to make them overflow): parity with the
+    oracle, every state stored once."""
+    net = gen.random_network(seed, nprocs=nprocs, states=(3, 6), outdeg=(1, 2), safety=False)
+    bits = net.firstbit()[-1]
+    assert (4 if bits <= 31 else (8 if bits <= 63 else 16)) == width
+    path = write_net(net, tmp_path, f"narrow{width}")
+    o = oracle(path, [], max_states=150_000)
+    assert o["states"] > 20_000
+    q_words = (int(o["states"] * slots_per_state) * width + 63) // 4
+    g = _gpu(gpu, path, {}, max_states=150_000, q_words=q_words, store_states=o["states"] + 64, collect_states=1)
+    _same(o, g)
+    assert g["table_count"] == g["states"]
+    assert g["slot_bytes"] == width and g["overflowed"] > 0
