@@ -62,9 +62,11 @@ def measured_peaks():
 
 
 def make_network_words():
+    """The network and its gpf words as a host buffer (32-bit words)."""
+    import numpy as np
     from gpuexplore_gb300 import gpf
     net = W.config2_network()
-    return net, gpf.encode(net)
+    return net, np.asarray(gpf.encode(net), dtype=np.uint32)
 
 
 def workload_config(budget, q_words, states, levels):

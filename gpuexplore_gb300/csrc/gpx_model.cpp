@@ -122,21 +122,20 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
         return "";
     };
 
-    // decode every (p, s) reachable in p's LTS from local state 0
-    struct PS {
-        std::vector<uint32_t> local;
-        std::vector<std::pair<uint32_t, std::vector<uint32_t>>> sync; // ascending action
-        std::vector<uint32_t> &targets_of(uint32_t a) {
-            auto it = std::lower_bound(sync.begin(), sync.end(), a,
-                                       [](const std::pair<uint32_t, std::vector<uint32_t>> &x, uint32_t v) {
-                                           return x.first < v;
-                                       });
-            if (it == sync.end() || it->first != a) it = sync.insert(it, {a, {}});
-            return it->second;
-        }
+    // Decode every (p, s) reachable in p's LTS from local state 0 into flat
+    // arrays: per state, its local targets (entry order, each once) and its
+    // synchronising (action, target) pairs (ascending action, entry order within
+    // an action, each pair once).  Ranges into the arrays per state; no
+    // allocation per state.
+    struct StateTr {
+        uint32_t lb, le, sb, se; // [lb, le) of loc, [sb, se) of sy
     };
-    std::vector<std::vector<PS>> ps(n);
+    std::vector<std::vector<StateTr>> tr(n);
+    std::vector<uint32_t> loc;
+    std::vector<uint64_t> sy; // action << 32 | target
     std::vector<uint32_t> nstates(n);
+    std::vector<uint32_t> todo;
+    std::vector<char> seen;
     for (uint32_t p = 0; p < n; p++) {
         const uint32_t nwords = g.proc_offsets_start[p + 1] - g.proc_offsets_start[p];
         const uint32_t nfields = nwords * per_off;
@@ -145,11 +144,12 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
         // every reachable local state s needs offset fields s and s+1, so state
         // indices are bounded by the input, whatever bits_state allows
         if (nfields < 2) return "transition offsets missing for a reachable local state";
-        std::vector<char> seen(nfields, 0);
-        std::vector<uint32_t> todo{0};
+        seen.assign(nfields, 0);
+        std::vector<StateTr> &trp = tr[p];
+        trp.assign(nfields, StateTr{0, 0, 0, 0});
+        todo.assign(1, 0);
         seen[0] = 1;
         uint32_t maxs = 0;
-        std::vector<PS> dec(nfields);
         while (!todo.empty()) {
             uint32_t s = todo.back();
             todo.pop_back();
@@ -157,43 +157,51 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
             if (s + 1 >= nfields) return "transition offsets missing for a reachable local state";
             uint32_t o1 = packed_field(base, s, g.nbits_offset);   // GPUexplore.cu:883-898
             uint32_t o2 = packed_field(base, s + 1, g.nbits_offset);
-            PS &rec = dec[s];
+            StateTr &t0 = trp[s];
+            t0.lb = (uint32_t)loc.size();
+            t0.sb = (uint32_t)sy.size();
             for (uint32_t k = o1; k < o2; k++) {
                 if (k >= g.nr_trans) return "transition range past proc_trans";
                 uint32_t e = g.proc_trans[k];
-                uint32_t ts[32], nts = 0;             // nslots <= 30
+                uint32_t nts = 0;
+                const uint64_t act = (uint64_t)((e >> 1) & ((1u << g.bits_act) - 1u)) << 32;
                 for (uint32_t i = 0; i < nslots; i++) {  // slots hold target+1 (GPUexplore.cu:159)
                     uint32_t t = (e >> (1 + g.bits_act + i * w)) & ((1u << w) - 1u);
                     if (!t) break;
-                    ts[nts++] = t - 1;
-                }
-                if (!nts) return "transition entry without targets";
-                std::vector<uint32_t> &dst =
-                    (e & 1u) ? rec.targets_of((e >> 1) & ((1u << g.bits_act) - 1u)) : rec.local;
-                for (uint32_t x = 0; x < nts; x++) {
-                    const uint32_t t = ts[x];
-                    if (std::find(dst.begin(), dst.end(), t) == dst.end()) dst.push_back(t);
+                    t -= 1;
+                    nts++;
+                    if (e & 1u) {
+                        const uint64_t at = act | t;
+                        if (std::find(sy.begin() + t0.sb, sy.end(), at) == sy.end()) sy.push_back(at);
+                    } else if (std::find(loc.begin() + t0.lb, loc.end(), t) == loc.end()) {
+                        loc.push_back(t);
+                    }
                     if (t + 1 >= nfields) return "transition offsets missing for a reachable local state";
                     if (!seen[t]) {
                         seen[t] = 1;
                         todo.push_back(t);
                     }
                 }
+                if (!nts) return "transition entry without targets";
             }
+            t0.le = (uint32_t)loc.size();
+            t0.se = (uint32_t)sy.size();
+            // group by action, keeping entry order within an action
+            std::stable_sort(sy.begin() + t0.sb, sy.end(),
+                             [](uint64_t x, uint64_t y) { return (x >> 32) < (y >> 32); });
         }
         nstates[p] = maxs + 1;
-        ps[p].resize(nstates[p]);
+        trp.resize(nstates[p]);
         for (uint32_t st = 0; st <= maxs; st++)
-            if (seen[st]) ps[p][st] = std::move(dec[st]);
+            if (!seen[st]) trp[st] = StateTr{0, 0, 0, 0};
     }
     if (state_bits > (uint32_t)kMaxStateBits) return "UNSUPPORTED: state vector wider than 126 bits";
 
     // rules, and per (p, s) the rules p leads (lowest member) for actions p has enabled
     std::vector<uint32_t> rule_mask, rule_act;
     std::vector<uint32_t> actions; // ascending, each once
-    for (uint32_t p = 0; p < n; p++)
-        for (auto &r : ps[p])
-            for (auto &kv : r.sync) actions.push_back(kv.first);
+    actions.reserve(sy.size());
+    for (uint64_t at : sy) actions.push_back((uint32_t)(at >> 32));
     std::sort(actions.begin(), actions.end());
     actions.erase(std::unique(actions.begin(), actions.end()), actions.end());
     std::vector<std::pair<uint32_t, uint32_t>> ranges(actions.size()); // per action: [first rule, count)
@@ -217,36 +225,39 @@ std::string decode_gpf(const Gpf &g, Decoded *out) {
     for (uint32_t p = 0; p < n; p++) {
         psbase[p] = (uint32_t)(recs.size() / kRecWords);
         for (uint32_t s = 0; s < nstates[p]; s++) {
-            const PS &r = ps[p][s];
+            const StateTr &r = tr[p][s];
             uint32_t rec[kRecWords] = {0};
             rec[R_LOFF] = (uint32_t)ltgt.size();
-            rec[R_LCNT] = (uint32_t)r.local.size();
-            for (uint32_t t : r.local) {
-                ltgt.push_back(t);
-                if (t == 1) rec[R_FLAGS] |= 1u;
+            rec[R_LCNT] = r.le - r.lb;
+            for (uint32_t k = r.lb; k < r.le; k++) {
+                ltgt.push_back(loc[k]);
+                if (loc[k] == 1) rec[R_FLAGS] |= 1u;
             }
             rec[R_SOFF] = (uint32_t)(sent.size() / 4);
-            rec[R_SCNT] = (uint32_t)r.sync.size();
             rec[R_ROFF] = (uint32_t)lrule.size();
-            uint32_t cl0 = 1u << p;
-            for (auto &kv : r.sync) {  // ascending action order
+            uint32_t cl0 = 1u << p, groups = 0;
+            for (uint32_t k = r.sb; k < r.se;) {  // one group per action, ascending
+                const uint32_t a = (uint32_t)(sy[k] >> 32);
                 uint32_t has1 = 0;
-                uint32_t toff = (uint32_t)stgt.size();
-                for (uint32_t t : kv.second) {
+                const uint32_t toff = (uint32_t)stgt.size();
+                for (; k < r.se && (uint32_t)(sy[k] >> 32) == a; k++) {
+                    const uint32_t t = (uint32_t)sy[k];
                     stgt.push_back(t);
                     if (t == 1) has1 = 1;
                 }
-                sent.push_back(kv.first);
+                const auto &rr = rules_range(a);
+                sent.push_back(a);
                 sent.push_back(toff);
-                sent.push_back((uint32_t)kv.second.size());
-                sent.push_back(has1 | (rules_range(kv.first).first << 1)); // + first rule of the action
-                auto rr = rules_range(kv.first);
-                for (uint32_t k = rr.first; k < rr.first + rr.second; k++) {
-                    uint32_t m = rule_mask[k];
+                sent.push_back((uint32_t)stgt.size() - toff);
+                sent.push_back(has1 | (rr.first << 1)); // + first rule of the action
+                for (uint32_t q = rr.first; q < rr.first + rr.second; q++) {
+                    uint32_t m = rule_mask[q];
                     if (m >> p & 1u) cl0 |= m; // GPUexplore.cu:1616-1624
-                    if ((uint32_t)__builtin_ctz(m) == p) lrule.push_back(k);
+                    if ((uint32_t)__builtin_ctz(m) == p) lrule.push_back(q);
                 }
+                groups++;
             }
+            rec[R_SCNT] = groups;
             rec[R_RCNT] = (uint32_t)lrule.size() - rec[R_ROFF];
             rec[R_CL0] = cl0;
             max_lrules = std::max(max_lrules, rec[R_RCNT]);

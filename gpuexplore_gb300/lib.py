@@ -247,7 +247,10 @@ class Model:
     @classmethod
     def from_words(cls, words: Sequence[int]) -> "Model":
         lib = load()
-        arr = np.ascontiguousarray(np.asarray(words, dtype=np.uint64).astype(np.uint32))
+        if isinstance(words, np.ndarray) and words.dtype == np.uint32:
+            arr = np.ascontiguousarray(words)  # a host buffer of gpf words, used in place
+        else:
+            arr = np.ascontiguousarray(np.asarray(words, dtype=np.uint64).astype(np.uint32))
         h = C.c_void_p()
         rc = lib.gpx_model_from_words(arr.ctypes.data_as(C.POINTER(C.c_uint32)), arr.size, C.byref(h))
         if rc != GPX_OK:
