@@ -231,7 +231,11 @@ template <class K, int MODE> __global__ void __launch_bounds__(256) place_kernel
     }
 }
 
-template <class K, int MODE> __global__ void __launch_bounds__(256, 4) explore_kernel(Params P) {
+// Plain mode: 4 blocks per SM (64 registers).  The POR modes: 3 blocks per SM,
+// whose 85 registers leave them without spills (config 3: 79.7 vs 80.5 ms with
+// 4 blocks and 124-172 bytes of spills).
+template <class K, int MODE>
+__global__ void __launch_bounds__(256, MODE == MODE_PLAIN ? 4 : 3) explore_kernel(Params P) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ LevelView view;
     const uint32_t *model = P.model;
