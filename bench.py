@@ -527,12 +527,17 @@ def main():
     # the same network (first 9 levels, 2 GB table; dram__bytes_read.sum +
     # dram__bytes_write.sum of one launch), scaled to this launch by the ratio of
     # algorithmic bytes (traffic grows with lookups, inserts and expanded states)
-    traffic, traffic_how = None, None
+    traffic, traffic_how, ncu_eff = None, None, None
     prof = os.path.join(ROOT, "profiles", "explore_kernel_config2_medium.json")
     if os.path.exists(prof):
         with open(prof) as f:
             pj = json.load(f)
         if pj.get("kernel_build") == KERNEL_BUILD:
+            # L2 sector efficiency of the probes and warp-execution efficiency of
+            # successor generation, from the same capture
+            ncu_eff = {"l2_read_sectors_per_request": pj["lts_read_sectors"] / pj["lts_read_requests"],
+                       "warp_execution_efficiency": pj["thread_instructions"] / (32.0 * pj["warp_instructions"]),
+                       "source": "profiles/explore_kernel_config2_medium.json"}
             scale = abytes / pj["algorithmic_bytes"]
             traffic = (pj["dram_bytes_read"] + pj["dram_bytes_write"]) * scale
             traffic_how = (f"ncu capture of the medium case ({pj['states']} states, one launch), x{scale:.3f} "
@@ -562,7 +567,13 @@ def main():
                      "kernel_ms": kms, "algorithmic_bytes": abytes,
                      "lookups": r["lookups"], "inserts": r["inserts"], "expanded": r["expanded"],
                      "probes": r["probes"],
+                     "ncu": ncu_eff,
                      "random_access": {"probes_per_s": r["probes"] / (kms / 1000.0),
+                                       # each probe reads a random sector; each insert also dirties
+                                       # it, so DRAM writes it back later: a second random access
+                                       "sector_accesses_per_s": (r["probes"] + r["inserts"]) / (kms / 1000.0),
+                                       "sector_accesses_frac_of_gather": (r["probes"] + r["inserts"]) /
+                                       (kms / 1000.0) / gathers,
                                        "peak_gathers_per_s": gathers, "peak_inserts_per_s": rmw,
                                        "floor_ms": floor_ms, "frac": floor_ms / kms,
                                        "how": "floor = inserts / insert-like rate + other probes / gather "
