@@ -38,9 +38,13 @@ struct BLevel {
 
 struct __align__(128) BInst {
     Ctrl ctrl;                      // counters, status, stop reason, done flag, level count
-    unsigned long long ticket;      // epoch << 40 | cursor
-    BLevel lvl[2];                  // the level of each epoch parity
-    unsigned long long completed[2];
+    // The ticket (polled by scanning warps, an atomic per claim), the completion
+    // counters (an atomic per claim) and the levels (read with every ticket) on
+    // lines of their own: sharing one line cost the ten config-1 rings in one
+    // batch 1.17 instead of 0.84 ms, config 5 430 instead of 386 ms.
+    alignas(128) unsigned long long ticket; // epoch << 40 | cursor
+    alignas(128) unsigned long long completed[2];
+    alignas(128) BLevel lvl[2];     // the level of each epoch parity
     unsigned long long finish_ns;
     // set up by the host
     void *table;                    // slots of the instance's width (kind)
@@ -753,6 +757,8 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
                       uint32_t level_capacity, gpx_batch_stats *stats) {
     if (!models || !jobs || !items || !opts || !count || opts->struct_size != sizeof(gpx_batch_options))
         return GPX_ERR_INVALID;
+    if (opts->threads < 0 || opts->threads % 32 || opts->threads > 256 || opts->load_factor > 0.95)
+        return GPX_ERR_INVALID; // refused before a GPU is looked for
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPX_ERR_NO_GPU;
     if (opts->device < 0 || opts->device >= ndev) return GPX_ERR_INVALID;
@@ -770,7 +776,6 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
     // and 24 worse); 0 switches the reservation off
     cfg.latency_sms = opts->latency_sms >= 0 ? opts->latency_sms : prop.multiProcessorCount / 10 + 1;
     cfg.prune_commuting = opts->prune_commuting != 0;
-    if (cfg.threads % 32 || cfg.threads > 256 || cfg.load_factor > 0.95) return GPX_ERR_INVALID;
     const int max_adm = opts->max_admissions > 0 ? opts->max_admissions : 3;
     gpx_batch_stats st;
     memset(&st, 0, sizeof st);
@@ -825,8 +830,10 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
         for (uint32_t i : sample) scap.push_back(cap[i]);
         double best = 1e30;
         BatchConfig bestc = cfg;
+        // (claims of 4 states suit batches of latency-bound rings, 16 the mixed
+        // config-5 batch: 0.79 / 385 ms against 0.83 / 415 ms with 8)
         for (int threads : {128, 256})
-            for (int claim : {8, 32, 64, 256})
+            for (int claim : {4, 8, 16, 32, 64, 256})
                 for (double lf : {0.25, 0.5}) {
                     BatchConfig c = cfg;
                     c.threads = threads;

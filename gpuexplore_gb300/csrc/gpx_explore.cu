@@ -58,16 +58,22 @@ namespace gpx {
 // arrive at the barrier, with all other blocks waiting).
 template <class K, int MODE> __device__ void close_phase(const Params &P) {
     Ctrl *c = P.ctrl;
-    if (MODE == MODE_PROVISO && c->phase == PH_DECIDE) {
+    // every field the close reads, loaded together before any store: one round
+    // trip to L2 instead of one per branch (config 1: 2.40 -> 2.33 ms)
+    const unsigned int ph = vload(&c->phase);
+    const unsigned long long ovf = vload(&c->overflow_count), hi = vload(&c->hi), sc = vload(&c->store_count);
+    const unsigned int nlev = vload(&c->nlevels), lvl = vload(&c->level), ll = vload(&c->launch_levels),
+                       err_read = vload(&c->error), viol = vload(&c->violation);
+    if (MODE == MODE_PROVISO && ph == PH_DECIDE) {
         c->phase = PH_EXPAND;
         c->cursor = 0;
         return;
     }
-    if (c->phase == PH_PLACE) { // the overflowed keys of this level are placed
+    if (ph == PH_PLACE) { // the overflowed keys of this level are placed
         c->place_ns += globaltimer() - c->place_t0;
         c->overflow_count = 0;
-    } else if (c->overflow_count) {
-        if (c->overflow_count <= P.overflow_cap && !c->error) {
+    } else if (ovf) {
+        if (ovf <= P.overflow_cap && !err_read) {
             // The level's inserts are done.  The exploration kernel returns and
             // place_kernel places the overflowed keys with every warp (PH_PLACE),
             // then closes the level; the relaunch continues with the next one.
@@ -76,7 +82,7 @@ template <class K, int MODE> __device__ void close_phase(const Params &P) {
             c->phase = PH_PLACE;
             c->cursor = 0;
             c->place_t0 = globaltimer();
-            c->overflowed += c->overflow_count;
+            c->overflowed += ovf;
             c->place_blocks = 0;
             if (P.claim) P.claim[0]++; // a new claim epoch (the counter survives runs)
             c->pause = 1;
@@ -85,10 +91,8 @@ template <class K, int MODE> __device__ void close_phase(const Params &P) {
         set_error(c, GPX_ERR_TABLE_FULL); // more keys than the overflow list holds
         c->overflow_count = 0;
     }
-    // the fields the decision reads, loaded together before any store
-    const unsigned long long hi = c->hi, sc = c->store_count;
-    const unsigned int nlev = c->nlevels, lvl = c->level, ll = c->launch_levels, err0 = c->error,
-                       viol = c->violation;
+    // placement or a full overflow list may have recorded an error since
+    const unsigned int err0 = (ph == PH_PLACE || ovf) ? vload(&c->error) : err_read;
     unsigned long long newhi = sc;
     if (newhi > P.store_cap) newhi = P.store_cap;
     unsigned long long cnt = newhi - hi;
@@ -164,12 +168,13 @@ template <class K, int MODE> __device__ void grid_barrier(const Params &P, Level
             asm volatile("red.release.gpu.global.add.u32 [%0], 1;" :: "l"(&c->bar_gen) : "memory");
         } else { // bounded wait for the close
             uint64_t t0 = globaltimer();
+            // polls at most 128 ns apart (512: config 1 2.35 -> 2.39 ms per ten rings)
             unsigned int ns = 32, g;
             for (;;) {
                 asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(&c->bar_gen) : "memory");
                 if (g != gen) break;
                 __nanosleep(ns);
-                if (ns < 512) ns <<= 1;
+                if (ns < 128) ns <<= 1;
                 if (globaltimer() - t0 > P.timeout_ns) {
                     set_error(c, GPX_ERR_TIMEOUT);
                     atomicMax(&c->timeout_at, 1u);

@@ -82,7 +82,7 @@ def test_batch_launch_shapes_and_autotune(gpu, tmp_path):
     assert stats["launches"] > 10
     items, stats = _check(gpu, tmp_path, cases, autotune=1)
     assert stats["kernel_iters"] in (0, 64, 512) and stats["narrow_slots"] in (0, 1)
-    assert stats["claim"] in (8, 32, 64, 256) and stats["tune_ms"] > 0
+    assert stats["claim"] in (4, 8, 16, 32, 64, 256) and stats["tune_ms"] > 0
     assert stats["p99_ms"] >= stats["p50_ms"] > 0
 
 

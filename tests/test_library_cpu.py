@@ -127,6 +127,20 @@ def test_option_defaults(built):
     assert b.prune_commuting == 1
 
 
+def test_batch_option_validation(built, tmp_path):
+    """gpx_batch_explore refuses bad launch options before it looks for a GPU."""
+    from gpuexplore_gb300 import lib
+    p = tmp_path / "m.gpf"
+    gpf.write(gen.ring(1), str(p))
+    m = lib.Model.from_file(str(p))
+    try:
+        for bad in (dict(threads=48), dict(threads=512), dict(threads=-32), dict(load_factor=0.99)):
+            items, stats = lib.batch_explore([m], [{"property": "deadlock"}], check=False, **bad)
+            assert stats["rc"] == 6, bad  # GPX_ERR_INVALID
+    finally:
+        m.close()
+
+
 def test_wide_local_state_fields_decode_in_bounded_memory(built):
     """A process whose declared bits_state far exceeds its state count: the
     decoder's reachability array is bounded by the gpf's offset fields, not by
