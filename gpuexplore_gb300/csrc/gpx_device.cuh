@@ -86,6 +86,7 @@ struct Params {
     uint32_t property;
     uint32_t levels_per_launch;
     uint32_t total_warps;
+    uint32_t batch_states;  // states in a warp's full batch (pairs per batch / processes, at most 32)
     uint32_t por_kind;      // POR_CAMPLE, POR_AMPLE or POR_STUBBORN
     // keys whose probe sequence was full, placed with eviction in a phase of their own
     void *overflow;

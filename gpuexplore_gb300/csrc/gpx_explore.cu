@@ -126,8 +126,13 @@ template <class K, int MODE> __device__ void close_phase(const Params &P) {
     c->cursor = 0;
     c->phase = (MODE == MODE_PROVISO) ? PH_DECIDE : PH_EXPAND;
     // claims shrink with the level (down to one state) so that small levels
-    // spread over every warp instead of queueing behind a few long batches
+    // spread over every warp instead of queueing behind a few long batches; a
+    // level that fits in one batch per warp is split into one static claim per
+    // warp (one-state claims from the cursor took a 36K-state level of the
+    // config-2 network 88 us)
     unsigned long long per = cnt / ((unsigned long long)P.total_warps * 4ull);
+    if (cnt <= (unsigned long long)P.total_warps * P.batch_states)
+        per = (cnt + P.total_warps - 1) / P.total_warps;
     c->claim = (unsigned int)(per < 1 ? 1 : (per > 4096 ? 4096 : per));
     if (P.levels_per_launch && ll + 1 >= P.levels_per_launch && !c->done) c->pause = 1;
 }
@@ -642,6 +647,13 @@ int upload_model(gpx_explorer *ex) {
     return GPX_OK;
 }
 
+// States in a warp's full batch: its (state, process) pairs over the processes.
+uint32_t batch_states_of(int mode, size_t nprocs) {
+    const size_t pairs = mode == MODE_PLAIN ? kPairMax : kPairMaxPor;
+    const size_t b = nprocs ? pairs / nprocs : 1;
+    return (uint32_t)std::max<size_t>(1, std::min<size_t>(32, b));
+}
+
 Params make_params(gpx_explorer *ex) {
     Params P;
     memset(&P, 0, sizeof P);
@@ -666,6 +678,7 @@ Params make_params(gpx_explorer *ex) {
     P.property = (uint32_t)ex->property;
     P.levels_per_launch = ex->o.kernel_iters > 0 ? (uint32_t)ex->o.kernel_iters : 0;
     P.total_warps = (uint32_t)(ex->blocks * (ex->threads / 32));
+    P.batch_states = batch_states_of(ex->mode, ex->model.dec.nstates.size());
     P.learned = (ex->o.por == 2 && ex->have_por_model) ? 1u : 0u;
     P.por_kind = por_kind_of(ex->o.por);
     P.por_model = ex->have_por_model ? ex->d_por_model : nullptr;
@@ -1600,6 +1613,7 @@ extern "C" int gpx_explore_noalloc(const gpx_model *model, const gpx_options *op
     P.property = (uint32_t)property;
     P.levels_per_launch = opts->kernel_iters > 0 ? (uint32_t)opts->kernel_iters : 0;
     P.total_warps = (uint32_t)(blocks * (threads / 32));
+    P.batch_states = batch_states_of(mode, model->dec.nstates.size());
     P.por_kind = por_kind_of(opts->por);
 
     // clear what must start at zero (the array keeps the previous call's contents;
