@@ -125,14 +125,17 @@ template <class K, int MODE> __device__ void close_phase(const Params &P) {
     c->hi = newhi;
     c->cursor = 0;
     c->phase = (MODE == MODE_PROVISO) ? PH_DECIDE : PH_EXPAND;
-    // claims shrink with the level (down to one state) so that small levels
-    // spread over every warp instead of queueing behind a few long batches; a
-    // level that fits in one batch per warp is split into one static claim per
-    // warp (one-state claims from the cursor took a 36K-state level of the
-    // config-2 network 88 us)
+    // Claims shrink with the level so that small levels spread over every warp
+    // instead of queueing behind a few long batches, but never below a full
+    // batch: a level that fits in one batch per warp is split into one static
+    // claim per warp, a larger one into claims of at least a batch.  (One-state
+    // claims from the cursor took a 36K-state level of the config-2 network
+    // 88 us, a 24K-state level of a config-3 network 70 us per phase.)
     unsigned long long per = cnt / ((unsigned long long)P.total_warps * 4ull);
     if (cnt <= (unsigned long long)P.total_warps * P.batch_states)
         per = (cnt + P.total_warps - 1) / P.total_warps;
+    else if (per < P.batch_states)
+        per = P.batch_states;
     c->claim = (unsigned int)(per < 1 ? 1 : (per > 4096 ? 4096 : per));
     if (P.levels_per_launch && ll + 1 >= P.levels_per_launch && !c->done) c->pause = 1;
 }
