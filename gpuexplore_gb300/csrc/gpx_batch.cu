@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <numeric>
 #include <vector>
 
 #include "gpx.h"
@@ -821,11 +822,16 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
                    cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, 32) == cudaSuccess;
 
     if (opts->autotune && todo.size() > 1) {
-        // tune on an evenly spaced sample of at most 48 instances
+        // tune on a sample of at most 64 instances, spread over the batch with a
+        // stride coprime to its size: an even stride over a batch whose job kinds
+        // alternate with the index sampled one kind only
         auto t0 = std::chrono::steady_clock::now();
         std::vector<uint32_t> sample;
-        size_t step = std::max<size_t>(1, todo.size() / 48);
-        for (size_t k = 0; k < todo.size() && sample.size() < 48; k += step) sample.push_back(todo[k]);
+        const size_t nt = todo.size(), want = std::min<size_t>(nt, 64);
+        size_t stride = std::max<size_t>(1, nt / want) | 1;
+        while (std::gcd(stride, nt) != 1) stride += 2;
+        for (size_t k = 0; k < want; k++) sample.push_back(todo[(k * stride) % nt]);
+        std::sort(sample.begin(), sample.end());
         std::vector<uint64_t> scap;
         for (uint32_t i : sample) scap.push_back(cap[i]);
         double best = 1e30;
@@ -879,6 +885,31 @@ int gpx_batch_explore(const gpx_model *const *models, const gpx_batch_job *jobs,
                 best = ms;
                 bestc = c;
             }
+        }
+        // Last, the claim size on the whole batch (at most 1,024 instances), at
+        // the sample's choice and two and four times it: a batch's makespan is
+        // set by its deepest instances, which a sample rarely holds (config 5:
+        // 608 ms with 16-state claims against 640 with the sample's 8).  A run in
+        // which an instance outgrew its partition still times the launch.
+        if (sample.size() < todo.size() && todo.size() <= 1024) {
+            double full_best = 1e30;
+            BatchConfig full_c = bestc;
+            std::vector<uint64_t> fcap; // admission capacities, in the order of todo
+            for (uint32_t i : todo) fcap.push_back(cap[i]);
+            for (int mul : {1, 2, 4}) {
+                BatchConfig c = bestc;
+                c.claim = bestc.claim * mul;
+                if (c.claim > 256) break;
+                std::vector<Outcome> o;
+                float ms = 0;
+                uint32_t l = 0;
+                const int r = run_launch(opts->device, prop, c, opts->seed, models, jobs, todo, fcap, d_por, &o, &ms, &l);
+                if ((r == GPX_OK || r == GPX_ERR_TABLE_FULL || r == GPX_ERR_STORE_FULL) && ms < full_best) {
+                    full_best = ms;
+                    full_c = c;
+                }
+            }
+            bestc = full_c;
         }
         cfg = bestc;
         st.tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
