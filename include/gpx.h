@@ -361,7 +361,8 @@ typedef struct {
                                a level: a quarter of a fair share per warp, up to 4096) */
     int32_t kernel_iters;   /* work claims per warp per launch (0 = until every instance is done) */
     int32_t autotune;       /* choose claim, threads, load factor, then kernel_iters, then the slot policy on a
-                               sample of the batch first (the explicit values above are the starting point) */
+                               sample of the batch, then the claim size on the whole batch (at most 1,024
+                               instances) first (the explicit values above are the starting point) */
     int32_t max_admissions; /* launches per instance before an overflow is final (0 = 3) */
     double load_factor;     /* table slots = admitted states / load_factor (0 = 0.5) */
     uint64_t seed;
