@@ -50,7 +50,7 @@ BUDGET = W.CONFIG2_BUDGET
 Q_WORDS = W.CONFIG2_Q_WORDS
 CPU_SAMPLE_BUDGET = W.CONFIG2_SAMPLE_BUDGET  # the first 9 BFS levels (38.8M states)
 WORKLOAD = "config-2 random gpf network (16 procs + monitor, seed 2024), -d, BFS to 1e8-state budget"
-KERNEL_BUILD = "place-kernel-v1"  # names the kernel version a committed traffic capture belongs to
+KERNEL_BUILD = "claim-rule-v2"  # names the kernel version a committed traffic capture belongs to
 
 
 def measured_peaks():
