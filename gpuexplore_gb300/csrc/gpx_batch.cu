@@ -92,10 +92,6 @@ struct BParams {
 constexpr unsigned long long kCriticalStates = 8192;
 constexpr unsigned int kCriticalEpochs = 32;
 
-static __device__ __forceinline__ unsigned long long vload64(const unsigned long long *p) {
-    return *(volatile const unsigned long long *)p;
-}
-
 // Acquire load of a ticket: the level it names is read after it.
 static __device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long *p) {
     unsigned long long v;

@@ -737,7 +737,7 @@ static int run(const gpf_t *m, const opts_t *o, result_t *res) {
 #pragma omp parallel reduction(| : violation)
             {
                 expand_t *x = (expand_t *)malloc(sizeof(expand_t));
-                sctx_t c = {m, o, shards, S, 0, 0, 1, NULL, 0, 0};
+                sctx_t c = {.m = m, .o = o, .shards = shards, .nshards = S, .cycle = 1}; /* the rest zero */
 #pragma omp for schedule(dynamic, 256)
                 for (int64_t i = 0; i < (int64_t)frontier.n; i++) {
                     int dl = 0;
@@ -759,7 +759,7 @@ static int run(const gpf_t *m, const opts_t *o, result_t *res) {
                 t = omp_get_thread_num();
 #endif
                 expand_t *x = (expand_t *)malloc(sizeof(expand_t));
-                sctx_t c = {m, o, shards, S, 0, 0, 0, outs + (size_t)t * S, 0, 0};
+                sctx_t c = {.m = m, .o = o, .shards = shards, .nshards = S, .out = outs + (size_t)t * S}; /* the rest zero */
 #pragma omp for schedule(dynamic, 256)
                 for (int64_t i = (int64_t)base; i < (int64_t)end; i++) {
                     const uint32_t *v = frontier.a + i * W;
