@@ -86,6 +86,16 @@ def test_batch_launch_shapes_and_autotune(gpu, tmp_path):
     assert stats["p99_ms"] >= stats["p50_ms"] > 0
 
 
+def test_batch_autotune_whole_batch_stage(gpu, tmp_path):
+    """A batch larger than the autotuner's 64-instance sample: after the sample
+    stages the claim size is chosen again on the whole batch (the sample's
+    choice, twice and four times it).  Every instance equals the oracle."""
+    cases = _batch_cases(72, 13)
+    items, stats = _check(gpu, tmp_path, cases, autotune=1)
+    assert stats["tune_ms"] > 0
+    assert stats["claim"] in (4, 8, 16, 32, 64, 128, 256, 512, 1024)
+
+
 def test_batch_pruning_on_and_off(gpu, tmp_path):
     """Plain instances prune commuting moves by default (the label array is the
     per-state array cycle-proviso instances use for clusters); with pruning off
