@@ -64,7 +64,7 @@ struct alignas(128) Ctrl {
     alignas(128) unsigned long long cursor;      // dynamic claims: offset beyond the static first claims
     alignas(128) unsigned long long store_count; // states appended to the store
     alignas(128) unsigned int bar_count;         // grid barrier arrivals
-    alignas(128) unsigned int bar_gen;           // grid barrier generation (polled by waiting blocks)
+    alignas(128) unsigned long long bar_word;    // grid barrier: generation and the next phase (polled)
     alignas(128) unsigned long long lookups; // statistics (one line)
     unsigned long long probes, expanded, inserts, inserts_lookups, pruned;
 };

@@ -54,9 +54,32 @@
 
 namespace gpx {
 
+// States per work claim of a level of `cnt` states.  Claims shrink with the
+// level so that small levels spread over every warp instead of queueing behind
+// a few long batches, but never below a full batch: a level that fits in one
+// batch per warp is split into one static claim per warp, a larger one into
+// claims of at least a batch.  (One-state claims from the cursor took a
+// 36K-state level of the config-2 network 88 us, a 24K-state level of a
+// config-3 network 70 us per phase.)
+__device__ __forceinline__ unsigned int claim_of(const Params &P, unsigned long long cnt) {
+    unsigned long long per = cnt / ((unsigned long long)P.total_warps * 4ull);
+    if (cnt <= (unsigned long long)P.total_warps * P.batch_states)
+        per = (cnt + P.total_warps - 1) / P.total_warps;
+    else if (per < P.batch_states)
+        per = P.batch_states;
+    return (unsigned int)(per < 1 ? 1 : (per > 4096 ? 4096 : per));
+}
+
+// What a close decided: the next phase, the end of its level, and whether the
+// kernel stops (done, paused or failed).
+struct Closed {
+    unsigned long long hi;
+    unsigned int phase, stop;
+};
+
 // Close the phase that every block has just finished (run by the last block to
 // arrive at the barrier, with all other blocks waiting).
-template <class K, int MODE> __device__ void close_phase(const Params &P) {
+template <class K, int MODE> __device__ Closed close_phase(const Params &P) {
     Ctrl *c = P.ctrl;
     // every field the close reads, loaded together before any store: one round
     // trip to L2 instead of one per branch (config 1: 2.40 -> 2.33 ms)
@@ -67,7 +90,7 @@ template <class K, int MODE> __device__ void close_phase(const Params &P) {
     if (MODE == MODE_PROVISO && ph == PH_DECIDE) {
         c->phase = PH_EXPAND;
         c->cursor = 0;
-        return;
+        return {hi, PH_EXPAND, err_read != 0};
     }
     if (ph == PH_PLACE) { // the overflowed keys of this level are placed
         c->place_ns += globaltimer() - c->place_t0;
@@ -86,7 +109,7 @@ template <class K, int MODE> __device__ void close_phase(const Params &P) {
             c->place_blocks = 0;
             if (P.claim) P.claim[0]++; // a new claim epoch (the counter survives runs)
             c->pause = 1;
-            return;
+            return {hi, PH_PLACE, 1u};
         }
         set_error(c, GPX_ERR_TABLE_FULL); // more keys than the overflow list holds
         c->overflow_count = 0;
@@ -108,36 +131,32 @@ template <class K, int MODE> __device__ void close_phase(const Params &P) {
     }
     c->level = lvl + 1;
     c->launch_levels = ll + 1;
-    if (err) {
+    constexpr unsigned int kGoOn = 0xFFFFFFFFu;
+    unsigned int stop = kGoOn;
+    if (err)
+        stop = GPX_STOP_ERROR;
+    else if (viol)
+        stop = GPX_STOP_VIOLATION;
+    else if (cnt == 0)
+        stop = GPX_STOP_DONE;
+    else if (P.max_states && newhi >= P.max_states)
+        stop = GPX_STOP_BUDGET;
+    if (stop != kGoOn) {
         c->done = 1;
-        c->stop = GPX_STOP_ERROR;
-    } else if (viol) {
-        c->done = 1;
-        c->stop = GPX_STOP_VIOLATION;
-    } else if (cnt == 0) {
-        c->done = 1;
-        c->stop = GPX_STOP_DONE;
-    } else if (P.max_states && newhi >= P.max_states) {
-        c->done = 1;
-        c->stop = GPX_STOP_BUDGET;
+        c->stop = stop;
     }
+    const unsigned int next = (MODE == MODE_PROVISO) ? PH_DECIDE : PH_EXPAND;
     c->lo = hi;
     c->hi = newhi;
     c->cursor = 0;
-    c->phase = (MODE == MODE_PROVISO) ? PH_DECIDE : PH_EXPAND;
-    // Claims shrink with the level so that small levels spread over every warp
-    // instead of queueing behind a few long batches, but never below a full
-    // batch: a level that fits in one batch per warp is split into one static
-    // claim per warp, a larger one into claims of at least a batch.  (One-state
-    // claims from the cursor took a 36K-state level of the config-2 network
-    // 88 us, a 24K-state level of a config-3 network 70 us per phase.)
-    unsigned long long per = cnt / ((unsigned long long)P.total_warps * 4ull);
-    if (cnt <= (unsigned long long)P.total_warps * P.batch_states)
-        per = (cnt + P.total_warps - 1) / P.total_warps;
-    else if (per < P.batch_states)
-        per = P.batch_states;
-    c->claim = (unsigned int)(per < 1 ? 1 : (per > 4096 ? 4096 : per));
-    if (P.levels_per_launch && ll + 1 >= P.levels_per_launch && !c->done) c->pause = 1;
+    c->phase = next;
+    c->claim = claim_of(P, cnt);
+    bool pause = false;
+    if (P.levels_per_launch && ll + 1 >= P.levels_per_launch && stop == kGoOn) {
+        c->pause = 1;
+        pause = true;
+    }
+    return {newhi, next, (stop != kGoOn || pause) ? 1u : 0u};
 }
 
 // What a block needs of the current phase, read from the control block once
@@ -155,6 +174,36 @@ __device__ __forceinline__ void read_view(const Ctrl *c, LevelView &v) {
     v.stop = vload(&c->done) | vload(&c->pause) | vload(&c->error);
 }
 
+// The barrier word the closer publishes: generation << 48 | stop << 47 |
+// phase << 45 | the level's end.  Waiters take the next phase from it instead
+// of reading the control block after the release (one L2 round trip less per
+// phase): the level's start is the previous end (or unchanged, from a decide
+// pass to its expand pass) and the claim size follows from the level's size
+// exactly as the closer computes it.  A phase field of 3 (an end past 2^45)
+// sends them to the control block.
+constexpr unsigned long long kEndMask = (1ull << 45) - 1ull;
+
+__device__ __forceinline__ unsigned long long phase_word(unsigned long long gen, const Closed &r) {
+    const unsigned int phase = r.hi > kEndMask ? 3u : r.phase;
+    return (gen << 48) | ((unsigned long long)(r.stop != 0) << 47) | ((unsigned long long)phase << 45) |
+           (r.hi & kEndMask);
+}
+
+template <int MODE> __device__ __forceinline__ void next_view(const Params &P, unsigned long long w, LevelView &v) {
+    const unsigned int phase = (unsigned int)(w >> 45) & 3u;
+    if (phase == 3u) {
+        read_view(P.ctrl, v);
+        return;
+    }
+    if (!(MODE == MODE_PROVISO && v.phase == PH_DECIDE && phase == PH_EXPAND)) { // a new level
+        v.lo = v.hi;
+        v.hi = w & kEndMask;
+        v.claim = claim_of(P, v.hi - v.lo);
+    }
+    v.phase = phase;
+    v.stop = (unsigned int)(w >> 47) & 1u;
+}
+
 // Grid-wide barrier; the last block to arrive closes the phase.  The wait is
 // bounded: after timeout_ns it records GPX_ERR_TIMEOUT and returns.  Thread 0
 // then refreshes the block's view of the next phase.
@@ -162,35 +211,37 @@ template <class K, int MODE> __device__ void grid_barrier(const Params &P, Level
     __syncthreads();
     if (threadIdx.x == 0) {
         Ctrl *c = P.ctrl;
-        unsigned int gen = vload(&c->bar_gen);
+        const unsigned long long w0 = vload(&c->bar_word);
         // The arrival releases this block's writes of the phase (its warps'
         // writes are ordered before it by the block barrier) and acquires the
-        // earlier arrivals'; the closer's release of bar_gen publishes the
-        // close to the waiters' acquire loads.  (Full fences around plain
-        // atomics did the same, 2.5% slower per level on config 1.)
+        // earlier arrivals'; the closer's release store of the barrier word
+        // publishes the close to the waiters' acquire loads.  (Full fences
+        // around plain atomics did the same, 2.5% slower per level on config 1.)
         unsigned int arrived;
         asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(arrived) : "l"(&c->bar_count) : "memory");
+        unsigned long long w;
         if (arrived == gridDim.x - 1) {
-            close_phase<K, MODE>(P);
+            w = phase_word((w0 >> 48) + 1ull, close_phase<K, MODE>(P));
             c->bar_count = 0;
-            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" :: "l"(&c->bar_gen) : "memory");
+            asm volatile("st.release.gpu.global.u64 [%0], %1;" :: "l"(&c->bar_word), "l"(w) : "memory");
         } else { // bounded wait for the close
             uint64_t t0 = globaltimer();
             // polls at most 128 ns apart (512: config 1 2.35 -> 2.39 ms per ten rings)
-            unsigned int ns = 32, g;
+            unsigned int ns = 32;
             for (;;) {
-                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(&c->bar_gen) : "memory");
-                if (g != gen) break;
+                asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(w) : "l"(&c->bar_word) : "memory");
+                if ((w >> 48) != (w0 >> 48)) break;
                 __nanosleep(ns);
                 if (ns < 128) ns <<= 1;
                 if (globaltimer() - t0 > P.timeout_ns) {
                     set_error(c, GPX_ERR_TIMEOUT);
                     atomicMax(&c->timeout_at, 1u);
+                    w = 3ull << 45; // the control block: its error stops the kernel
                     break;
                 }
             }
         }
-        read_view(c, view);
+        next_view<MODE>(P, w, view);
     }
     __syncthreads();
 }
@@ -239,7 +290,7 @@ template <class K, int MODE> __global__ void __launch_bounds__(256) place_kernel
         __threadfence();
         if (atomicAdd(&c->place_blocks, 1u) == gridDim.x - 1) { // the last block: every key is placed
             __threadfence();
-            close_phase<K, MODE>(P);
+            (void)close_phase<K, MODE>(P);
         }
     }
 }
