@@ -14,6 +14,16 @@ EXP sync vectors   ``"a" * "b" * _ -> "c"``: one label (or ``_`` = does not take
                    transition whose label is in no vector for that LTS is blocked,
                    except the internal action, which stays local.
 
+EXP operators     an operand of the composition may be wrapped in
+                   ``hide L1, ... in <operand> end hide`` (those labels become the
+                   internal action), ``hide all but L1, ... in ... end hide`` (every
+                   other label does) or ``rename L1 -> M1, ... in ... end rename``;
+                   the innermost wrapper applies first.  Hiding or renaming around
+                   the whole ``par`` only relabels the composed transitions, which
+                   leaves the state space and the verdicts unchanged, so such outer
+                   wrappers are accepted as they are.  A ``par`` nested inside an
+                   operand is not supported.
+
 Mapping to gpf: a vector with one participant turns that LTS's transitions on
 its label into local transitions; a vector with two or more participants
 becomes one synchronising action whose single rule is the participant set, and
@@ -71,15 +81,72 @@ def parse_aut(text: str) -> Aut:
 _LBL = r'"(?:[^"\\]|\\.)*"|_|[A-Za-z0-9_.!?:-]+'
 
 
+# an operand: (.aut file name, [(operator, argument)] innermost first)
+Operand = Tuple[str, List[Tuple[str, object]]]
+
+
+def _label_list(text: str) -> List[str]:
+    labs = [x.strip() for x in text.split(",") if x.strip()]
+    for x in labs:
+        if not re.fullmatch(_LBL, x) or x == "_":
+            raise ValueError(f"bad label {x!r}")
+    return [x.strip('"') for x in labs]
+
+
+def parse_operand(text: str) -> Operand:
+    """An operand of the parallel composition: an .aut file name, possibly under
+    hide / rename wrappers."""
+    t = text.strip()
+    m = re.fullmatch(r"hide\s+(all\s+but\s+)?(.*?)\s+in\s+(.*)\s+end\s+hide", t, flags=re.S)
+    if m:
+        name, ops = parse_operand(m.group(3))
+        return name, ops + [("hide_all_but" if m.group(1) else "hide", _label_list(m.group(2)))]
+    m = re.fullmatch(r"rename\s+(.*?)\s+in\s+(.*)\s+end\s+rename", t, flags=re.S)
+    if m:
+        pairs = {}
+        for item in m.group(1).split(","):
+            if not item.strip():
+                continue
+            if "->" not in item:
+                raise ValueError(f"bad renaming {item!r}")
+            a, b = (x.strip() for x in item.split("->", 1))
+            (a,), (b,) = _label_list(a), _label_list(b)
+            pairs[a] = b
+        name, ops = parse_operand(m.group(2))
+        return name, ops + [("rename", pairs)]
+    if re.search(r"\b(par|hide|rename)\b", t):
+        raise ValueError(f"unsupported operand {t!r} (a nested par, or a malformed hide / rename)")
+    return t.strip('"'), []
+
+
+def apply_ops(aut: Aut, ops: Sequence[Tuple[str, object]]) -> Aut:
+    """The LTS with the operand's hide / rename wrappers applied, innermost first."""
+    trans = list(aut.trans)
+    for op, arg in ops:
+        if op == "hide":
+            trans = [(s, INTERNAL[0] if lab in arg else lab, d) for s, lab, d in trans]
+        elif op == "hide_all_but":
+            trans = [(s, lab if (lab in arg or lab in INTERNAL) else INTERNAL[0], d) for s, lab, d in trans]
+        else:
+            trans = [(s, arg.get(lab, lab), d) for s, lab, d in trans]
+    return Aut(aut.initial, aut.nstates, trans)
+
+
 def parse_exp(text: str) -> Tuple[List[List[Optional[str]]], List[str]]:
     """Return (vectors, lts file names) of a `par using ... in ... end par` expression."""
+    vectors, ops = parse_exp_operands(text)
+    return vectors, [name for name, _ in ops]
+
+
+def parse_exp_operands(text: str) -> Tuple[List[List[Optional[str]]], List[Operand]]:
+    """Return (vectors, operands) of a `par using ... in ... end par` expression."""
     body = re.sub(r"\(\*.*?\*\)", " ", text, flags=re.S)  # comments
     m = re.search(r"\bpar\s+using\b(.*?)\bin\b(.*?)\bend\s+par\b", body, flags=re.S)
     if not m:
         raise ValueError("expected: par using <vectors> in <lts> || ... end par")
     vec_text, lts_text = m.groups()
-    names = [re.sub(r'^"|"$', "", x.strip()) for x in lts_text.split("||")]
-    names = [n for n in names if n]
+    operands = [parse_operand(x) for x in lts_text.split("||") if x.strip()]
+    names = [name for name, _ in operands]
     vectors: List[List[Optional[str]]] = []
     for item in re.split(r",(?=(?:[^\"]*\"[^\"]*\")*[^\"]*$)", vec_text):
         item = item.strip()
@@ -95,7 +162,7 @@ def parse_exp(text: str) -> Tuple[List[List[Optional[str]]], List[str]]:
         if len(vec) != len(names):
             raise ValueError(f"vector {item!r} has {len(vec)} elements for {len(names)} LTSs")
         vectors.append(vec)
-    return vectors, names
+    return vectors, operands
 
 
 def to_network(auts: Sequence[Aut], vectors: Sequence[Sequence[Optional[str]]]) -> Network:
@@ -140,12 +207,12 @@ def to_network(auts: Sequence[Aut], vectors: Sequence[Sequence[Optional[str]]]) 
 
 def convert(exp_path: str, out_path: str) -> Network:
     with open(exp_path) as f:
-        vectors, names = parse_exp(f.read())
+        vectors, operands = parse_exp_operands(f.read())
     base = os.path.dirname(os.path.abspath(exp_path))
     auts = []
-    for nm in names:
+    for nm, ops in operands:
         with open(os.path.join(base, nm)) as f:
-            auts.append(parse_aut(f.read()))
+            auts.append(apply_ops(parse_aut(f.read()), ops))
     net = to_network(auts, vectors)
     write(net, out_path)
     return net

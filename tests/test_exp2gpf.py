@@ -77,6 +77,90 @@ def test_aut_parsing_errors():
         exp2gpf.parse_exp('par using "a" * _ -> "a" in "x.aut" end par')  # vector length
 
 
+P_AUT = 'des (0, 3, 3)\n(0, "u", 1)\n(1, "w", 2)\n(2, i, 0)\n'
+Q_AUT = 'des (0, 3, 3)\n(0, "a", 1)\n(1, "v", 2)\n(2, "v", 0)\n'
+VEC = '"a" * "a" -> s, _ * "v" -> v'
+
+# (EXP text, the test's own reading: per operand, a relabelling applied to its labels)
+OPERAND_CASES = [
+    (f'par using {VEC} in "p.aut" || "q.aut" end par', [{}, {}]),
+    (f'par using {VEC} in rename "u" -> "a" in "p.aut" end rename || "q.aut" end par', [{"u": "a"}, {}]),
+    (f'par using {VEC} in hide "w" in rename "u" -> "a" in "p.aut" end rename end hide || "q.aut" end par',
+     [{"u": "a", "w": "i"}, {}]),
+    (f'par using {VEC} in rename "u" -> "a" in hide all but "u" in "p.aut" end hide end rename || "q.aut" end par',
+     [{"u": "a", "w": "i"}, {}]),
+    (f'par using {VEC} in "p.aut" || hide "v" in "q.aut" end hide end par', [{}, {"v": "i"}]),
+    # around the whole composition: relabels the composed transitions only
+    (f'hide s, v in par using {VEC} in rename "u" -> "a" in "p.aut" end rename || "q.aut" end par end hide',
+     [{"u": "a"}, {}]),
+]
+
+
+def _product(auts, vectors):
+    """BFS over tuples of states, the EXP par-using semantics (as product_explore)."""
+    import itertools
+    n = len(auts)
+    out = [{} for _ in range(n)]
+    for k, a in enumerate(auts):
+        for src, lab, dst in a.trans:
+            out[k].setdefault(src, []).append((lab, dst))
+    init = tuple(a.initial for a in auts)
+    seen, frontier, levels = {init}, [init], [1]
+    while frontier:
+        nxt = []
+        for st in frontier:
+            succ = []
+            for k in range(n):
+                for lab, dst in out[k].get(st[k], []):
+                    if lab in exp2gpf.INTERNAL or any(v[k] == lab and sum(x is not None for x in v) == 1 for v in vectors):
+                        succ.append(st[:k] + (dst,) + st[k + 1:])
+            for v in vectors:
+                parts = [k for k in range(n) if v[k] is not None]
+                if len(parts) < 2:
+                    continue
+                choices = [[dst for lab, dst in out[k].get(st[k], []) if lab == v[k]] for k in parts]
+                for combo in itertools.product(*choices):
+                    t = list(st)
+                    for k, dst in zip(parts, combo):
+                        t[k] = dst
+                    succ.append(tuple(t))
+            for t in succ:
+                if t not in seen:
+                    seen.add(t)
+                    nxt.append(t)
+        if nxt:
+            levels.append(len(nxt))
+        frontier = nxt
+    return len(seen), levels
+
+
+@pytest.mark.parametrize("case", range(len(OPERAND_CASES)))
+def test_hide_and_rename_operands(built, tmp_path, case):
+    """Operands under hide / rename, and wrappers around the whole composition:
+    the converted network against a product explorer that applies the same
+    relabellings by itself."""
+    text, relabel = OPERAND_CASES[case]
+    (tmp_path / "p.aut").write_text(P_AUT)
+    (tmp_path / "q.aut").write_text(Q_AUT)
+    (tmp_path / "n.exp").write_text(text)
+    out = str(tmp_path / "n.gpf")
+    exp2gpf.convert(str(tmp_path / "n.exp"), out)
+    vectors = [["a", "a"], [None, "v"]]
+    auts = []
+    for raw, rl in zip((P_AUT, Q_AUT), relabel):
+        a = exp2gpf.parse_aut(raw)
+        a.trans = [(src, rl.get(lab, lab), dst) for src, lab, dst in a.trans]
+        auts.append(a)
+    states, levels = _product(auts, vectors)
+    o = oracle(out, [])
+    assert (o["states"], o["levels"]) == (states, levels), text
+
+
+def test_nested_par_is_refused():
+    with pytest.raises(ValueError):
+        exp2gpf.parse_exp('par using "a" * "a" in "p.aut" || par using "b" in "q.aut" end par end par')
+
+
 @pytest.mark.gpu
 def test_philosophers_on_gpu(gpu, tmp_path):
     out = str(tmp_path / "phil.gpf")
