@@ -22,7 +22,10 @@ EXP operators     an operand of the composition may be wrapped in
                    the whole ``par`` only relabels the composed transitions, which
                    leaves the state space and the verdicts unchanged, so such outer
                    wrappers are accepted as they are.  A ``par`` nested inside an
-                   operand is not supported.
+                   operand is flattened onto its leaf LTSs: an outer vector element
+                   naming an inner result label (``-> b``) stands for every inner
+                   vector with that result; inner vectors whose result is internal
+                   fire without outer partners.
 
 Mapping to gpf: a vector with one participant turns that LTS's transitions on
 its label into local transitions; a vector with two or more participants
@@ -33,6 +36,7 @@ explores from the all-zero vector).
 """
 from __future__ import annotations
 
+import itertools
 import os
 import re
 import sys
@@ -84,85 +88,218 @@ _LBL = r'"(?:[^"\\]|\\.)*"|_|[A-Za-z0-9_.!?:-]+'
 # an operand: (.aut file name, [(operator, argument)] innermost first)
 Operand = Tuple[str, List[Tuple[str, object]]]
 
+_TOKEN = re.compile(r'\s*(\|\||->|\*|,|"(?:[^"\\]|\\.)*"|[A-Za-z0-9_.!?:-]+)')
+_KEYWORDS = {"par", "using", "in", "end", "hide", "all", "but", "rename"}
 
-def _label_list(text: str) -> List[str]:
-    labs = [x.strip() for x in text.split(",") if x.strip()]
-    for x in labs:
-        if not re.fullmatch(_LBL, x) or x == "_":
-            raise ValueError(f"bad label {x!r}")
-    return [x.strip('"') for x in labs]
+
+def _tokens(text: str) -> List[str]:
+    body = re.sub(r"\(\*.*?\*\)", " ", text, flags=re.S)  # comments
+    out, pos = [], 0
+    while pos < len(body):
+        if body[pos:].strip() == "":
+            break
+        m = _TOKEN.match(body, pos)
+        if not m:
+            raise ValueError(f"unexpected text near {body[pos:pos + 20]!r}")
+        out.append(m.group(1))
+        pos = m.end()
+    return out
+
+
+class _Parser:
+    """Recursive descent over the EXP subset: par using / hide / rename / .aut leaves."""
+
+    def __init__(self, text: str):
+        self.t, self.k = _tokens(text), 0
+
+    def peek(self, off: int = 0) -> Optional[str]:
+        return self.t[self.k + off] if self.k + off < len(self.t) else None
+
+    def take(self, want: Optional[str] = None) -> str:
+        tok = self.peek()
+        if tok is None or (want is not None and tok != want):
+            raise ValueError(f"expected {want or 'more input'}, found {tok!r}")
+        self.k += 1
+        return tok
+
+    def label(self) -> str:
+        tok = self.take()
+        if tok in _KEYWORDS or tok in ("||", "->", "*", ",", "_"):
+            raise ValueError(f"expected a label, found {tok!r}")
+        return tok.strip('"')
+
+    def labels(self) -> List[str]:
+        out = [self.label()]
+        while self.peek() == ",":
+            self.take(",")
+            out.append(self.label())
+        return out
+
+    def expr(self):
+        tok = self.peek()
+        if tok == "par":
+            self.take("par")
+            self.take("using")
+            vectors = [self.vector()]
+            while self.peek() == ",":
+                self.take(",")
+                vectors.append(self.vector())
+            self.take("in")
+            ops = [self.expr()]
+            while self.peek() == "||":
+                self.take("||")
+                ops.append(self.expr())
+            self.take("end")
+            self.take("par")
+            for elems, _ in vectors:
+                if len(elems) != len(ops):
+                    raise ValueError(f"a vector has {len(elems)} elements for {len(ops)} operands")
+            return ("par", vectors, ops)
+        if tok == "hide":
+            self.take("hide")
+            all_but = self.peek() == "all" and self.peek(1) == "but"
+            if all_but:
+                self.take("all")
+                self.take("but")
+            labs = self.labels()
+            self.take("in")
+            e = self.expr()
+            self.take("end")
+            self.take("hide")
+            return ("hide_all_but" if all_but else "hide", labs, e)
+        if tok == "rename":
+            self.take("rename")
+            pairs = {}
+            while True:
+                a = self.label()
+                self.take("->")
+                pairs[a] = self.label()
+                if self.peek() != ",":
+                    break
+                self.take(",")
+            self.take("in")
+            e = self.expr()
+            self.take("end")
+            self.take("rename")
+            return ("rename", pairs, e)
+        return ("leaf", self.label())
+
+    def vector(self):
+        elems = [self.elem()]
+        while self.peek() == "*":
+            self.take("*")
+            elems.append(self.elem())
+        result = None
+        if self.peek() == "->":
+            self.take("->")
+            result = self.label()
+        return elems, result
+
+    def elem(self) -> Optional[str]:
+        if self.peek() == "_":
+            self.take("_")
+            return None
+        return self.label()
+
+
+def _relabel(lab: str, op: str, arg) -> str:
+    if lab in INTERNAL:
+        return lab
+    if op == "hide":
+        return INTERNAL[0] if lab in arg else lab
+    if op == "hide_all_but":
+        return lab if lab in arg else INTERNAL[0]
+    return arg.get(lab, lab)
+
+
+def _flatten(node, ops=()):
+    """(leaves, moves) of an expression: leaves are (file, wrappers) operands;
+    moves are None for a leaf (it offers its own labels), else the composite's
+    transitions as (one label or None per leaf, result label).  Wrappers on a
+    composite act on its result labels; on a leaf they are applied to its LTS."""
+    kind = node[0]
+    if kind == "leaf":  # `ops` lists the wrappers outermost first; a leaf applies the innermost first
+        return [(node[1], list(reversed(ops)))], None
+    if kind in ("hide", "hide_all_but", "rename"):
+        leaves, moves = _flatten(node[2], ops + ((kind, node[1]),))
+        if moves is None:
+            return leaves, None
+        return leaves, [(el, _relabel(r, kind, node[1])) for el, r in moves]
+    _, vectors, operands = node
+    parts = [_flatten(o) for o in operands]
+    offs, n = [], 0
+    for leaves, _ in parts:
+        offs.append(n)
+        n += len(leaves)
+    leaves_all = [lf for leaves, _ in parts for lf in leaves]
+    moves: List[Tuple[List[Optional[str]], str]] = []
+    for elems, result in vectors:
+        options = []
+        for i, e in enumerate(elems):
+            if e is None:
+                continue
+            leaves, sub = parts[i]
+            if sub is None:
+                options.append([{offs[i]: e}])
+            else:  # a composite operand: any of its moves with that result label
+                options.append([{offs[i] + k: x for k, x in enumerate(el) if x is not None} for el, r in sub if r == e])
+        if not options:
+            continue
+        present = [e for e in elems if e is not None]
+        res = result if result is not None else (present[0] if len(set(present)) == 1 else "_".join(present))
+        for combo in itertools.product(*options):
+            vec: List[Optional[str]] = [None] * n
+            for part in combo:
+                for k, x in part.items():
+                    vec[k] = x
+            moves.append((vec, res))
+    for i, (leaves, sub) in enumerate(parts):  # an operand's internal moves need no partner
+        if sub is None:
+            continue
+        for el, r in sub:
+            if r in INTERNAL:
+                vec = [None] * n
+                for k, x in enumerate(el):
+                    vec[offs[i] + k] = x
+                moves.append((vec, r))
+    return leaves_all, moves
 
 
 def parse_operand(text: str) -> Operand:
-    """An operand of the parallel composition: an .aut file name, possibly under
-    hide / rename wrappers."""
-    t = text.strip()
-    m = re.fullmatch(r"hide\s+(all\s+but\s+)?(.*?)\s+in\s+(.*)\s+end\s+hide", t, flags=re.S)
-    if m:
-        name, ops = parse_operand(m.group(3))
-        return name, ops + [("hide_all_but" if m.group(1) else "hide", _label_list(m.group(2)))]
-    m = re.fullmatch(r"rename\s+(.*?)\s+in\s+(.*)\s+end\s+rename", t, flags=re.S)
-    if m:
-        pairs = {}
-        for item in m.group(1).split(","):
-            if not item.strip():
-                continue
-            if "->" not in item:
-                raise ValueError(f"bad renaming {item!r}")
-            a, b = (x.strip() for x in item.split("->", 1))
-            (a,), (b,) = _label_list(a), _label_list(b)
-            pairs[a] = b
-        name, ops = parse_operand(m.group(2))
-        return name, ops + [("rename", pairs)]
-    if re.search(r"\b(par|hide|rename)\b", t):
-        raise ValueError(f"unsupported operand {t!r} (a nested par, or a malformed hide / rename)")
-    return t.strip('"'), []
+    """One .aut operand, possibly under hide / rename wrappers."""
+    leaves, moves = _flatten(_Parser(text).expr())
+    if moves is not None or len(leaves) != 1:
+        raise ValueError("expected a single .aut operand")
+    return leaves[0]
 
 
 def apply_ops(aut: Aut, ops: Sequence[Tuple[str, object]]) -> Aut:
     """The LTS with the operand's hide / rename wrappers applied, innermost first."""
     trans = list(aut.trans)
     for op, arg in ops:
-        if op == "hide":
-            trans = [(s, INTERNAL[0] if lab in arg else lab, d) for s, lab, d in trans]
-        elif op == "hide_all_but":
-            trans = [(s, lab if (lab in arg or lab in INTERNAL) else INTERNAL[0], d) for s, lab, d in trans]
-        else:
-            trans = [(s, arg.get(lab, lab), d) for s, lab, d in trans]
+        trans = [(s, _relabel(lab, op, arg), d) for s, lab, d in trans]
     return Aut(aut.initial, aut.nstates, trans)
 
 
 def parse_exp(text: str) -> Tuple[List[List[Optional[str]]], List[str]]:
-    """Return (vectors, lts file names) of a `par using ... in ... end par` expression."""
+    """Return (vectors, lts file names) of an EXP network."""
     vectors, ops = parse_exp_operands(text)
     return vectors, [name for name, _ in ops]
 
 
 def parse_exp_operands(text: str) -> Tuple[List[List[Optional[str]]], List[Operand]]:
-    """Return (vectors, operands) of a `par using ... in ... end par` expression."""
-    body = re.sub(r"\(\*.*?\*\)", " ", text, flags=re.S)  # comments
-    m = re.search(r"\bpar\s+using\b(.*?)\bin\b(.*?)\bend\s+par\b", body, flags=re.S)
-    if not m:
-        raise ValueError("expected: par using <vectors> in <lts> || ... end par")
-    vec_text, lts_text = m.groups()
-    operands = [parse_operand(x) for x in lts_text.split("||") if x.strip()]
-    names = [name for name, _ in operands]
-    vectors: List[List[Optional[str]]] = []
-    for item in re.split(r",(?=(?:[^\"]*\"[^\"]*\")*[^\"]*$)", vec_text):
-        item = item.strip()
-        if not item:
-            continue
-        left = item.split("->")[0]
-        parts = [p.strip() for p in left.split("*")]
-        vec = []
-        for p in parts:
-            if not re.fullmatch(_LBL, p):
-                raise ValueError(f"bad vector element {p!r}")
-            vec.append(None if p == "_" else p.strip('"'))
-        if len(vec) != len(names):
-            raise ValueError(f"vector {item!r} has {len(vec)} elements for {len(names)} LTSs")
-        vectors.append(vec)
-    return vectors, operands
+    """Return (vectors over the leaf LTSs, leaf operands) of an EXP network:
+    nested compositions are flattened -- an outer vector element naming an inner
+    result label stands for every inner vector with that result -- and inner
+    vectors whose result is internal fire without outer partners."""
+    p = _Parser(text)
+    root = p.expr()
+    if p.peek() is not None:
+        raise ValueError(f"unexpected {p.peek()!r} after the expression")
+    leaves, moves = _flatten(root)
+    if moves is None:
+        raise ValueError("expected: par using <vectors> in <operand> || ... end par")
+    return [el for el, _ in moves], leaves
 
 
 def to_network(auts: Sequence[Aut], vectors: Sequence[Sequence[Optional[str]]]) -> Network:

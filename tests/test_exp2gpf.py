@@ -156,9 +156,54 @@ def test_hide_and_rename_operands(built, tmp_path, case):
     assert (o["states"], o["levels"]) == (states, levels), text
 
 
-def test_nested_par_is_refused():
-    with pytest.raises(ValueError):
-        exp2gpf.parse_exp('par using "a" * "a" in "p.aut" || par using "b" in "q.aut" end par end par')
+P3 = 'des (0, 2, 2)\n(0, "a", 1)\n(1, "u", 0)\n'
+Q3 = 'des (0, 3, 3)\n(0, "a", 1)\n(1, "v", 2)\n(2, i, 0)\n'
+R3 = 'des (0, 2, 2)\n(0, "b", 1)\n(1, "v", 0)\n'
+INNER = 'par using "a" * "b" -> x, "v" * "v" -> {v} in "q.aut" || "r.aut" end par'
+FLAT = 'par using {vecs} in "p.aut" || "q.aut" || "r.aut" end par'
+
+# (a nested network, the same network written flat over p, q, r)
+NESTED_CASES = [
+    ('par using "a" * "x" -> s, "u" * _ -> u, _ * "v" -> w in "p.aut" || ' + INNER.format(v="v") + ' end par',
+     FLAT.format(vecs='"a" * "a" * "b" -> s, "u" * _ * _ -> u, _ * "v" * "v" -> w')),
+    # an inner vector with the internal result fires without an outer partner
+    ('par using "a" * "x" -> s, "u" * _ -> u in "p.aut" || ' + INNER.format(v="i") + ' end par',
+     FLAT.format(vecs='"a" * "a" * "b" -> s, "u" * _ * _ -> u, _ * "v" * "v" -> i')),
+    # hiding an inner result: the inner move becomes internal, the outer vector on it never fires
+    ('par using "a" * "x" -> s, "u" * _ -> u, _ * "v" -> w in "p.aut" || hide x in ' + INNER.format(v="v") +
+     ' end hide end par',
+     FLAT.format(vecs='"u" * _ * _ -> u, _ * "v" * "v" -> w, _ * "a" * "b" -> i')),
+    # renaming an inner result
+    ('par using "a" * "y" -> s, "u" * _ -> u, _ * "v" -> w in "p.aut" || rename x -> y in ' + INNER.format(v="v") +
+     ' end rename end par',
+     FLAT.format(vecs='"a" * "a" * "b" -> s, "u" * _ * _ -> u, _ * "v" * "v" -> w')),
+]
+
+
+@pytest.mark.parametrize("case", range(len(NESTED_CASES)))
+def test_nested_par_equals_flat(built, tmp_path, case):
+    """A par nested inside an operand is flattened onto its leaf LTSs: an outer
+    vector element naming an inner result label stands for the inner vectors
+    with that result.  Each nested network explores exactly like its flat form."""
+    nested, flat = NESTED_CASES[case]
+    for name, text in (("p.aut", P3), ("q.aut", Q3), ("r.aut", R3), ("nested.exp", nested), ("flat.exp", flat)):
+        (tmp_path / name).write_text(text)
+    exp2gpf.convert(str(tmp_path / "nested.exp"), str(tmp_path / "nested.gpf"))
+    exp2gpf.convert(str(tmp_path / "flat.exp"), str(tmp_path / "flat.gpf"))
+    a, b = oracle(str(tmp_path / "nested.gpf"), []), oracle(str(tmp_path / "flat.gpf"), [])
+    assert (a["states"], a["levels"], a["set_hash"]) == (b["states"], b["levels"], b["set_hash"])
+    vectors, _ = exp2gpf.parse_exp(flat)
+    auts = [exp2gpf.parse_aut(t) for t in (P3, Q3, R3)]
+    assert (a["states"], a["levels"]) == _product(auts, vectors)
+
+
+def test_exp_syntax_errors():
+    for bad in ('par using "a" * "a" in "p.aut" end par',             # two elements, one operand
+                'par using "a" in "p.aut" || end par',                # missing operand
+                'hide in "p.aut" end hide',                           # no label
+                '"p.aut"'):                                           # no composition
+        with pytest.raises(ValueError):
+            exp2gpf.parse_exp(bad)
 
 
 @pytest.mark.gpu
