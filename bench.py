@@ -69,10 +69,14 @@ def make_network_words():
     return net, np.asarray(gpf.encode(net), dtype=np.uint32)
 
 
-def workload_config(budget, q_words, states, levels):
+PROPERTY_FLAG = {"deadlock": "-d", "safety": "-p"}
+
+
+def workload_config(budget, q_words, states, levels, prop="deadlock"):
     """The `config` object both arms print: the workload only (network,
     property, budget, table size) and the size of its result."""
-    return {"workload": WORKLOAD, "property": "deadlock (-d)", "budget": budget, "q_words": q_words,
+    workload = WORKLOAD if prop == "deadlock" else WORKLOAD.replace(", -d,", ", -p,")
+    return {"workload": workload, "property": f"{prop} ({PROPERTY_FLAG[prop]})", "budget": budget, "q_words": q_words,
             "table_gb": q_words * 4 / 1e9, "states": states, "levels": levels,
             "l2": "inputs larger than L2 (20 GB hash table, reset every step)"}
 
@@ -150,16 +154,16 @@ def job_value(states_per_rank, step_ms, world):
     return states_per_rank * world / (step_ms / 1000.0)
 
 
-def cpu_oracle_run(path, threads, budget):
+def cpu_oracle_run(path, threads, budget, prop="deadlock"):
     from gpuexplore_gb300.build import ORACLE
-    out = subprocess.run([ORACLE, path, "-d", "--threads", str(threads), "--max-states", str(budget)],
+    out = subprocess.run([ORACLE, path, PROPERTY_FLAG[prop], "--threads", str(threads), "--max-states", str(budget)],
                          capture_output=True, text=True, check=True)
     return json.loads(out.stdout)
 
 
-def cpu_single_thread(path):
+def cpu_single_thread(path, prop="deadlock"):
     """The oracle on one thread over the named sample (the first 9 levels)."""
-    o = cpu_oracle_run(path, 1, CPU_SAMPLE_BUDGET)
+    o = cpu_oracle_run(path, 1, CPU_SAMPLE_BUDGET, prop)
     return {"value": o["states"] / o["seconds"], "unit": "states/s", "cores": 1, "seconds": o["seconds"],
             "sample": f"first {len(o['levels'])} BFS levels ({o['states']} states) of the same network"}
 
@@ -179,13 +183,13 @@ def run_reference(args, rank, world):
         path = os.path.join(d, "c2.gpf")
         gpf.write(net, path)
         for _ in range(args.warmup):
-            cpu_oracle_run(path, threads, CPU_SAMPLE_BUDGET)
+            cpu_oracle_run(path, threads, CPU_SAMPLE_BUDGET, args.property)
         secs, results = [], []
         for _ in range(args.steps):
-            o = cpu_oracle_run(path, threads, args.budget)
+            o = cpu_oracle_run(path, threads, args.budget, args.property)
             secs.append(o["seconds"])
             results.append(o)
-        single = cpu_single_thread(path)
+        single = cpu_single_thread(path, args.property)
     o = results[-1]
     for x in results:  # deterministic whatever the thread schedule
         assert (x["states"], x["levels"], x["set_hash"]) == (o["states"], o["levels"], o["set_hash"])
@@ -195,7 +199,7 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": "new states/s", "value": v, "unit": "states/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(secs) / len(secs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": workload_config(args.budget, args.q_words, o["states"], len(o["levels"])),
+            "config": workload_config(args.budget, args.q_words, o["states"], len(o["levels"]), args.property),
             "cpu_baseline": {"value": v, "unit": "states/s", "cores": threads, "kind": "port", "sample": sample,
                              "set_hash": o["set_hash"], "single_thread": single},
             "e2e": {"value": v, "unit": "states/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -426,6 +430,8 @@ def main():
     ap.add_argument("--q-words", type=int, default=None,
                     help="hash table size in 32-bit words (default: the workload's own)")
     ap.add_argument("--store-states", type=int, default=0, help="state store capacity (0: table slots)")
+    ap.add_argument("--property", default="deadlock", choices=["deadlock", "safety"],
+                    help="the headline network's property: -d (default) or -p")
     ap.add_argument("--workload", default="config2",
                     choices=["config1", "config2", "config3", "config4", "config5", "liveness"],
                     help="config2 is the headline; the others print their own line")
@@ -463,7 +469,7 @@ def main():
     net, words = make_network_words()
     sv_nints = (net.firstbit()[-1] + 1 + 31) // 32  # the reference's words per vector
     model = lib.Model.from_words(words)
-    base = dict(property="deadlock", q_words=args.q_words, max_states=args.budget, store_states=args.store_states,
+    base = dict(property=args.property, q_words=args.q_words, max_states=args.budget, store_states=args.store_states,
                 device=local, launch_graph=0 if args.no_graph else 1)
     # Device-timed runs compute the visited-set hash after the timed interval, so
     # that every run can be checked against the others and against the oracle.
@@ -553,7 +559,7 @@ def main():
         "metric": "new states/s", "value": value, "unit": "states/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded gpf generator)",
-        "config": workload_config(args.budget, args.q_words, r["states"], len(r["levels"])),
+        "config": workload_config(args.budget, args.q_words, r["states"], len(r["levels"]), args.property),
         "parallelism": f"replicas x{world}",
         "launch": {"slot_bytes": r["slot_bytes"], "blocks": r["blocks"], "threads": r["threads"],
                    "table_reset": {"how": "generation tag in every slot" if r["table_generation"] else "clear",
@@ -593,8 +599,8 @@ def main():
         with tempfile.TemporaryDirectory() as d:
             path = os.path.join(d, "c2.gpf")
             gpf.write(net, path)
-            o = cpu_oracle_run(path, threads, args.budget)
-            single = cpu_single_thread(path)
+            o = cpu_oracle_run(path, threads, args.budget, args.property)
+            single = cpu_single_thread(path, args.property)
         # the oracle checks the GPU run: same states, per-level counts and visited set
         parity_ok = (o["states"], o["levels"], o["set_hash"]) == (r["states"], r["levels"], r["set_hash"])
         line["cpu_baseline"] = {"value": o["states"] / o["seconds"], "unit": "states/s", "cores": threads,
